@@ -1,0 +1,272 @@
+/*
+ * rts_scatter.h -- C ABI of the GB300 scattering-integral library
+ * (librts_scatter.so).
+ *
+ * The library computes the scattering integral of the radiation-transport
+ * source iteration of relativistic_solver_hllc,
+ *
+ *     S[k][c] = sum_j W[j][k] * Ibar[j][c],   Ibar[j][c] = (1/4) sum_f Illum[j][c][f]
+ *     W[j][k] = Gamma(w_j, w_k) * area_j / full_area      (Thomson, reference form)
+ *
+ * followed (optionally) by the source update S <- (1-lambda) B + lambda S,
+ * plus the FP64 direction moments (energy, flux) and the FP64 convergence
+ * residual.  Data layouts are the reference's: Illum is [direction][cell][face]
+ * FP64 (grid_t::Illum, solve_module/solve_global_struct.h:153-230) and the
+ * scattering array is [local out-direction][cell] FP64 (grid_t::scattering).
+ *
+ * Every entry point returns an rts_status; none calls exit().  Sizes and
+ * offsets are 64-bit.  A context is used by one host thread at a time.
+ * Reference paths below are relative to solver_hllc_illum_cuda/.
+ */
+#ifndef RTS_SCATTER_H
+#define RTS_SCATTER_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTS_ABI_VERSION 1
+
+typedef enum rts_status {
+    RTS_OK = 0,
+    RTS_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, range outside the grid */
+    RTS_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
+    RTS_ERR_OUT_OF_MEMORY = 3,    /* device or pinned host allocation failed */
+    RTS_ERR_BAD_STATE = 4,        /* call out of order (e.g. scatter before init) */
+    RTS_ERR_TIMEOUT = 5,          /* a host-side wait reached its deadline */
+    RTS_ERR_OVER_BUDGET = 6,      /* allocation refused by the HBM budget */
+    RTS_ERR_UNSUPPORTED = 7,      /* mode not built for this device / size */
+    RTS_ERR_DEVICE_WAIT = 8       /* a bounded device-side wait gave up */
+} rts_status;
+
+/* Stream slots: e_cuda_stream_id_t (solve_module/solve_global_struct.h:234-240),
+ * created with the same priorities as SetDevice (cuda/cuda_solve.cu:46-67). */
+typedef enum rts_stream_id {
+    RTS_STREAM_SCATTERING_1 = 0,
+    RTS_STREAM_SCATTERING_2 = 1,
+    RTS_STREAM_PARAMS = 2,
+    RTS_STREAM_COUNT = 3
+} rts_stream_id;
+
+/* Direction-pair kernels. */
+typedef enum rts_phase {
+    RTS_PHASE_THOMSON = 0, /* Gamma = 3(1+mu^2)/4, W = Gamma*area_j/full_area (cuda/cuda_utils.cu:7-16) */
+    RTS_PHASE_HG = 1,      /* Henyey-Greenstein, each out-direction column renormalised to sum 1 */
+    RTS_PHASE_CUSTOM = 2   /* W supplied by the caller (rts_set_weights) */
+} rts_phase;
+
+/* Arithmetic of the contraction. */
+typedef enum rts_precision {
+    RTS_PREC_FP64 = 0,   /* FP64 CUDA cores; matches the CPU integral to 1e-12 relative */
+    RTS_PREC_BF16X3 = 1, /* tcgen05 tensor cores, split BF16 hi/lo, three products, FP32 accumulate */
+    RTS_PREC_FP16X3 = 2  /* tcgen05 tensor cores, scaled split FP16 hi/lo, three products, FP32 accumulate */
+} rts_precision;
+
+typedef struct rts_ctx rts_ctx;
+
+/* ---------------------------------------------------------------------- */
+/* context, devices, streams                                               */
+/* ---------------------------------------------------------------------- */
+
+int rts_abi_version(void);
+
+/* Replaces SetDevice (cuda/cuda_solve.cu:46-67): selects the device and
+ * creates the three priority streams. */
+int rts_ctx_create(int device, rts_ctx** out);
+
+/* Replaces ClearDevice + ClearHost (cuda/cuda_struct.cu:180-214): frees every
+ * device and pinned host buffer of the context.  Accepts NULL. */
+int rts_ctx_destroy(rts_ctx* ctx);
+
+/* Text of the last error raised on this context ("" if none). */
+const char* rts_last_error(const rts_ctx* ctx);
+
+/* Cap on the device bytes this context may hold (default: 90% of the
+ * device memory free at creation).  Allocations beyond it fail with
+ * RTS_ERR_OVER_BUDGET. */
+int rts_set_hbm_budget(rts_ctx* ctx, int64_t bytes);
+int rts_hbm_used(const rts_ctx* ctx, int64_t* bytes);
+
+/* ---------------------------------------------------------------------- */
+/* grid and directions                                                     */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces InitDevice (cuda/cuda_struct.cu:134-178,187-190) for the
+ * scattering path.  Directions: xyz [M][3], area [M], full_area
+ * (grid_directions_t, global_def.h:79-90).  Allocates device Illum
+ * [M][N][4], device scattering [end-start][N] for the local out-directions
+ * [start, end), and the pinned host Illum / scattering arrays that InitDevice
+ * hands to grid_t (cuda/cuda_struct.cu:154-156).  The phase kernel defaults
+ * to RTS_PHASE_THOMSON. */
+int rts_init(rts_ctx* ctx, const double* xyz, const double* area, int64_t M, double full_area,
+             int64_t N, int64_t start, int64_t end);
+
+/* Pinned host arrays owned by the context (grid_t::Illum, grid_t::scattering). */
+int rts_host_illum(rts_ctx* ctx, double** illum);
+int rts_host_scattering(rts_ctx* ctx, double** scattering);
+
+/* Phase kernel for later integrals (recomputes the FP64 W). */
+int rts_set_phase(rts_ctx* ctx, int phase, double g);
+
+/* Caller-supplied W[j][k] for j in [0, M), k in the local out-directions
+ * (row-major, (end-start) columns).  Sets the phase to RTS_PHASE_CUSTOM. */
+int rts_set_weights(rts_ctx* ctx, const double* W);
+
+/* ---------------------------------------------------------------------- */
+/* Illum transfer                                                          */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces CudaSendIllumAsync(size, shift_dev, shift_host, Illum_host)
+ * (cuda/cuda_solve.cu:77-83) and, with shift_dev == shift_host, the
+ * two-argument overload (:69-76).  Counts are in doubles; the copy goes on
+ * stream RTS_STREAM_SCATTERING_1 as in the reference (cuda_streams[0]). */
+int rts_send_illum_async(rts_ctx* ctx, int64_t size, int64_t shift_dev, int64_t shift_host,
+                         const double* illum_host);
+
+/* Replaces CopyIllumOnDevice (cuda/cuda_solve.cu:85-88): synchronous copy of
+ * the first `size` doubles. */
+int rts_copy_illum(rts_ctx* ctx, int64_t size, const double* illum_host);
+
+/* ---------------------------------------------------------------------- */
+/* scattering integral (FP64, the drop-in path)                            */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces CalculateIntScatteringAsyncMPIStream (cuda/cuda_solve.cu:89-111,
+ * kernel d_GetS_MPI_Stream at cuda/cuda_kernel.cu:82-111): computes local
+ * out-directions [start, end) on `stream` and queues the D2H of rows
+ * [start, end) to host_out + start*N (host_out NULL: the pinned host
+ * scattering array).  The reference offsets the copy by `start` elements,
+ * which is right only for start == 0; this entry point uses start*N. */
+int rts_scattering_async(rts_ctx* ctx, int64_t start, int64_t end, int stream, double* host_out);
+
+/* Replaces CalculateIntScattering (cuda/cuda_solve.cu:153-170): copies
+ * illum_host (all M*N*4 doubles; NULL: the pinned host Illum) to the device,
+ * computes every local out-direction and copies the result to host_out
+ * (NULL: the pinned host scattering array), synchronously. */
+int rts_scattering(rts_ctx* ctx, const double* illum_host, double* host_out);
+
+/* Copies rows [start, end) of the device scattering array to host_out +
+ * start*N on `stream` without recomputing them (the D2H half of
+ * CalculateIntScatteringAsyncMPIStream, cuda/cuda_solve.cu:107-108). */
+int rts_read_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, double* host_out);
+
+/* One evaluation with host buffers at the given precision (rts_precision):
+ * copies illum_host (M*N*4 doubles, reference layout) and B_host (N values)
+ * to the device, computes S = (1-lambda) B + lambda W^T Ibar for every local
+ * out-direction and copies S (FP64, [local][N]) to S_host, synchronously.
+ * With lambda = 1 and B ignored this is CalculateIntScattering at the
+ * requested precision. */
+int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
+                          const double* B_host, double lambda, double* S_host);
+
+/* Device pointers of the resident arrays (for callers that keep data on the
+ * GPU): Illum [M][N][4] and scattering [end-start][N]. */
+int rts_device_arrays(rts_ctx* ctx, double** d_illum, double** d_scattering);
+
+/* ---------------------------------------------------------------------- */
+/* moments, update, residual                                               */
+/* ---------------------------------------------------------------------- */
+
+/* Energy E[c] = sum_j Ibar*area_j/full_area and flux F[c][3] =
+ * sum_j w_j Ibar*area_j/full_area in FP64 (cuda/cuda_utils.cu:18-67,
+ * cuda/cuda_kernel.cu:113-134), on `stream`; results copied to the host
+ * arrays that are non-NULL, synchronously with that stream. */
+int rts_moments(rts_ctx* ctx, int stream, double* energy, double* flux);
+
+/* S <- (1-lambda) B[c] + lambda S on the device scattering array
+ * (local rows [start, end)), and the FP64 residual max|S_new - S_old|
+ * against the values it replaces (residual may be NULL). */
+int rts_source_update(rts_ctx* ctx, const double* B_host, double lambda, int64_t start,
+                      int64_t end, int stream, double* residual);
+
+/* ---------------------------------------------------------------------- */
+/* synchronisation                                                         */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces CudaSyncStream (cuda/cuda_solve.cu:37-40) with a deadline:
+ * timeout_us < 0 waits without limit, otherwise RTS_ERR_TIMEOUT when the
+ * stream's work has not finished in time (the work keeps running). */
+int rts_sync_stream(rts_ctx* ctx, int stream, int64_t timeout_us);
+
+/* Replaces CudaWait (cuda/cuda_solve.cu:42-45) with a deadline. */
+int rts_wait(rts_ctx* ctx, int64_t timeout_us);
+
+/* ---------------------------------------------------------------------- */
+/* device-resident source iteration                                        */
+/* ---------------------------------------------------------------------- */
+
+/* Prepares a source iteration on the Illum already on the device:
+ * precision (rts_precision), source B [N] (host, FP64), albedo lambda.
+ * Requires the local out-directions to be all M directions.  For the tensor
+ * precisions this builds the split operands of W and Ibar on the device. */
+int rts_solve_setup(rts_ctx* ctx, int precision, const double* B_host, double lambda);
+
+/* One evaluation: S_int = W^T Ibar, S = (1-lambda) B + lambda S_int,
+ * residual = max|S - S_prev| (FP64, S_prev = 0 before the first step); then,
+ * if relax != 0, Ibar <- 0.5 Ibar + 0.5 S for the next step.  All on
+ * RTS_STREAM_SCATTERING_1; *residual (may be NULL) is read back, which
+ * synchronises the stream. */
+int rts_solve_step(rts_ctx* ctx, int relax, double* residual);
+
+/* Same step with nothing read back (for timing loops); the residual of the
+ * step stays on the device and rts_solve_residual fetches it. */
+int rts_solve_step_async(rts_ctx* ctx, int relax);
+int rts_solve_residual(rts_ctx* ctx, double* residual);
+
+/* Residuals of the last n steps since rts_solve_setup, oldest first
+ * (n <= 4096). */
+int rts_solve_residual_history(rts_ctx* ctx, double* out, int64_t n);
+
+/* Copies the current S [M][N] (FP64) to the host. */
+int rts_solve_read(rts_ctx* ctx, double* S_host);
+
+/* Copies the first `size` doubles of the device Illum to the host (the
+ * reverse of rts_copy_illum), synchronously. */
+int rts_read_illum(rts_ctx* ctx, int64_t size, double* illum_host);
+
+/* Copies the current face-mean intensity Ibar [M][N] (FP64) to the host. */
+int rts_solve_read_ibar(rts_ctx* ctx, double* ibar_host);
+
+/* ---------------------------------------------------------------------- */
+/* synthetic inputs (benchmark workloads; not part of the reference API)   */
+/* ---------------------------------------------------------------------- */
+
+/* Fills the device Illum with lognormal(mu, sigma) values from the same
+ * counter hash as the CPU generator (stream 1, index j*N+c, or
+ * (j*N+c)*4+f with independent_faces). */
+int rts_synth_illum(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int independent_faces);
+
+/* Spherical Fibonacci direction set: xyz [M][3], area [M] = 4 pi / M,
+ * full_area = 4 pi (host only, no context needed). */
+int rts_synth_directions(int64_t M, double* xyz, double* area, double* full_area);
+
+/* uniform(lo, hi) values of counter-hash stream `stream`, indices
+ * [i0, i0 + n) (host only). */
+int rts_synth_uniform(uint64_t seed, uint64_t stream, double lo, double hi, int64_t i0, int64_t n,
+                      double* out);
+
+/* ---------------------------------------------------------------------- */
+/* instrumentation                                                         */
+/* ---------------------------------------------------------------------- */
+
+/* The cudaStream_t of a stream slot (for callers that order their own work
+ * or record CUDA events against the library's streams). */
+int rts_stream_handle(rts_ctx* ctx, int stream, void** handle);
+
+/* Number of kernels this context has launched so far. */
+int rts_launch_count(const rts_ctx* ctx, int64_t* count);
+
+/* CUDA-event timing of the dominant kernel of each integral (the FP64
+ * scattering kernel or the tensor-core contraction), recorded on the stream
+ * it is launched on.  enable != 0 turns recording on and clears the totals;
+ * total_ms / launches (may be NULL) return what was recorded so far, after
+ * synchronising the recorded events. */
+int rts_kernel_timing(rts_ctx* ctx, int enable, double* total_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTS_SCATTER_H */

@@ -1,0 +1,275 @@
+"""CPU oracle of the scattering path -- TEST INFRASTRUCTURE ONLY.
+
+Python binding of oracle/scatter_oracle.c (the C restatement of the
+reference's CPU scattering integral, moments and direction partition) and of
+oracle/_ref/libref_scatter.so (the reference's own functions, compiled from the
+reference source text where that tree exists).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg import this package;
+the product library never does.
+
+Parity pin: tests/golden/ holds outputs of the reference's own functions
+(generated by tests/golden/make_golden.py through libref_scatter.so); the
+restatement is checked against them in tests/test_oracle.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+BUILD_DIR = ORACLE_DIR / "_build"
+LIB_PATH = BUILD_DIR / "liborc.so"
+REF_DIR = ORACLE_DIR / "_ref"
+REF_LIB = REF_DIR / "libref_scatter.so"
+REFERENCE_ROOT = Path(os.environ.get("RTS_REFERENCE_ROOT", "/root/reference"))
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i64 = C.c_int64
+_i64p = C.POINTER(C.c_int64)
+_u64 = C.c_uint64
+
+
+def build(force: bool = False) -> Path:
+    """Compile the C restatement (gcc -O3 -fopenmp) into oracle/_build/liborc.so."""
+    src = ORACLE_DIR / "scatter_oracle.c"
+    BUILD_DIR.mkdir(exist_ok=True)
+    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
+        return LIB_PATH
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler found for the oracle")
+    tmp = LIB_PATH.with_suffix(".so.tmp")
+    cmd = [cc, "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(src), "-o", str(tmp), "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_ref() -> Path | None:
+    """Compile the reference's own functions (only where the reference tree exists)."""
+    if not (REFERENCE_ROOT / "solver_hllc_illum_cuda").is_dir():
+        return None
+    script = ORACLE_DIR / "build_ref.sh"
+    res = subprocess.run(["sh", str(script)], capture_output=True, text=True,
+                         env={**os.environ, "RTS_REFERENCE_ROOT": str(REFERENCE_ROOT)})
+    if res.returncode != 0:
+        raise RuntimeError(f"reference build failed:\n{res.stdout}\n{res.stderr}")
+    return REF_LIB
+
+
+_SIG = {
+    "orc_uniform": (C.c_double, [_u64, _u64, _u64]),
+    "orc_normal": (C.c_double, [_u64, _u64, _u64]),
+    "orc_fill_illum": (None, [_u64, C.c_double, C.c_double, _i64, _i64, _i64, C.c_int, _dp]),
+    "orc_fill_uniform": (None, [_u64, _u64, C.c_double, C.c_double, _i64, _i64, _dp]),
+    "orc_fill_illum_cells": (None, [_u64, C.c_double, C.c_double, _i64, _i64, _i64, _i64, C.c_int, _dp]),
+    "orc_fibonacci_directions": (None, [_i64, _dp, _dp, _dp]),
+    "orc_weights_thomson": (None, [_i64, _dp, _dp, C.c_double, _i64, _i64, _dp]),
+    "orc_weights_hg": (None, [_i64, _dp, _dp, C.c_double, _i64, _i64, _dp]),
+    "orc_gets": (C.c_double, [_dp, _i64, _i64, _dp, _dp, C.c_double, _dp, _i64]),
+    "orc_calculate_int_cpu": (None, [_i64, _i64, _dp, _dp, C.c_double, _dp, _i64, _i64, _dp, C.c_int]),
+    "orc_calculate_int_cells": (None, [_i64, _i64, _dp, _dp, C.c_double, _dp, _i64, _i64, _i64p, _i64, _dp, C.c_int]),
+    "orc_scatter_matrix": (None, [_dp, _i64, _i64, _dp, _i64, _dp, C.c_int]),
+    "orc_face_mean": (None, [_dp, _i64, _i64, _dp]),
+    "orc_energy": (None, [_dp, _i64, _i64, _dp, C.c_double, _dp]),
+    "orc_stream": (None, [_dp, _i64, _i64, _dp, _dp, C.c_double, _dp]),
+    "orc_source_update": (None, [_i64, _i64, _dp, _dp, C.c_double]),
+    "orc_max_abs_diff": (C.c_double, [_dp, _dp, _i64]),
+    "orc_iterate": (None, [_dp, _i64, _dp, _i64, _dp, C.c_double, C.c_int, C.c_int, _dp, _dp]),
+    "orc_get_send": (None, [C.c_int, C.c_int, _ip]),
+    "orc_get_disp": (None, [C.c_int, C.c_int, _ip]),
+    "orc_max_threads": (C.c_int, []),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB_PATH))
+        for n, (r, a) in _SIG.items():
+            f = getattr(L, n)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+# ---------------------------------------------------------------- inputs
+def fibonacci_directions(M: int):
+    xyz = np.empty(3 * M)
+    area = np.empty(M)
+    fa = C.c_double()
+    lib().orc_fibonacci_directions(M, _p(xyz), _p(area), C.byref(fa))
+    return xyz.reshape(M, 3), area, fa.value
+
+
+def illum(seed: int, mu: float, sigma: float, N: int, M: int, j0: int = 0, j1: int | None = None,
+          independent_faces: bool = False) -> np.ndarray:
+    j1 = M if j1 is None else j1
+    out = np.empty((j1 - j0) * N * 4)
+    lib().orc_fill_illum(seed, mu, sigma, N, j0, j1, int(independent_faces), _p(out))
+    return out
+
+
+def illum_cells_into(out: np.ndarray, seed: int, mu: float, sigma: float, N: int, M: int, c0: int, c1: int,
+                     independent_faces: bool = False) -> None:
+    """Fill cells [c0, c1) of a full [M][N][4] array (others untouched)."""
+    assert out.dtype == np.float64 and out.size >= M * N * 4
+    lib().orc_fill_illum_cells(seed, mu, sigma, N, M, c0, c1, int(independent_faces), _p(out))
+
+
+def uniform(seed: int, stream: int, lo: float, hi: float, n: int, i0: int = 0) -> np.ndarray:
+    out = np.empty(n)
+    lib().orc_fill_uniform(seed, stream, lo, hi, i0, n, _p(out))
+    return out
+
+
+def weights_thomson(xyz, area, full_area, k0: int = 0, Mout: int | None = None) -> np.ndarray:
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    M = area.size
+    Mout = M - k0 if Mout is None else Mout
+    W = np.empty(M * Mout)
+    lib().orc_weights_thomson(M, _p(xyz), _p(area), full_area, k0, Mout, _p(W))
+    return W.reshape(M, Mout)
+
+
+def weights_hg(xyz, area, g: float, k0: int = 0, Mout: int | None = None) -> np.ndarray:
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    M = area.size
+    Mout = M - k0 if Mout is None else Mout
+    W = np.empty(M * Mout)
+    lib().orc_weights_hg(M, _p(xyz), _p(area), g, k0, Mout, _p(W))
+    return W.reshape(M, Mout)
+
+
+# ---------------------------------------------------------------- integrals
+def calculate_int_cpu(N, xyz, area, full_area, illum_arr, disp_loc=0, size_loc=None, nthreads=0):
+    """Restated CalculateIntCPU: scattering [size_loc][N] (FP64)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    illum_arr = np.ascontiguousarray(illum_arr, dtype=np.float64)
+    M = area.size
+    size_loc = M - disp_loc if size_loc is None else size_loc
+    out = np.empty(size_loc * N)
+    lib().orc_calculate_int_cpu(N, M, _p(xyz), _p(area), full_area, _p(illum_arr), disp_loc, size_loc,
+                                _p(out), nthreads)
+    return out.reshape(size_loc, N)
+
+
+def calculate_int_cells(N, xyz, area, full_area, illum_arr, cells, disp_loc=0, size_loc=None, nthreads=0):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int64)
+    M = area.size
+    size_loc = M - disp_loc if size_loc is None else size_loc
+    out = np.empty(size_loc * cells.size)
+    lib().orc_calculate_int_cells(N, M, _p(xyz), _p(area), full_area, _p(illum_arr), disp_loc, size_loc,
+                                  cells.ctypes.data_as(_i64p), cells.size, _p(out), nthreads)
+    return out.reshape(size_loc, cells.size)
+
+
+def scatter_matrix(W, Ibar, nthreads=0) -> np.ndarray:
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    Ibar = np.ascontiguousarray(Ibar, dtype=np.float64)
+    Min, Mout = W.shape
+    N = Ibar.size // Min
+    out = np.empty(Mout * N)
+    lib().orc_scatter_matrix(_p(W), Min, Mout, _p(Ibar), N, _p(out), nthreads)
+    return out.reshape(Mout, N)
+
+
+def face_mean(illum_arr, N, M) -> np.ndarray:
+    illum_arr = np.ascontiguousarray(illum_arr, dtype=np.float64)
+    out = np.empty(M * N)
+    lib().orc_face_mean(_p(illum_arr), N, M, _p(out))
+    return out.reshape(M, N)
+
+
+def energy(illum_arr, N, area, full_area) -> np.ndarray:
+    illum_arr = np.ascontiguousarray(illum_arr, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    out = np.empty(N)
+    lib().orc_energy(_p(illum_arr), N, area.size, _p(area), full_area, _p(out))
+    return out
+
+
+def stream(illum_arr, N, xyz, area, full_area) -> np.ndarray:
+    illum_arr = np.ascontiguousarray(illum_arr, dtype=np.float64)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    out = np.empty(3 * N)
+    lib().orc_stream(_p(illum_arr), N, area.size, _p(xyz), _p(area), full_area, _p(out))
+    return out.reshape(N, 3)
+
+
+def source_update(S, B, lam) -> np.ndarray:
+    S = np.array(S, dtype=np.float64, copy=True, order="C")
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    Mout, N = S.shape
+    lib().orc_source_update(N, Mout, _p(S), _p(B), lam)
+    return S
+
+
+def iterate(W, Ibar_cells, B_cells, lam, iters, relax=True):
+    """FP64 source iteration on a subset of cells; Ibar_cells [M][ncell]."""
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    I = np.array(Ibar_cells, dtype=np.float64, copy=True, order="C")
+    B = np.ascontiguousarray(B_cells, dtype=np.float64)
+    M, ncell = I.shape
+    S = np.empty(M * ncell)
+    res = np.empty(iters)
+    lib().orc_iterate(_p(W), M, _p(I), ncell, _p(B), lam, iters, int(relax), _p(S), _p(res))
+    return S.reshape(M, ncell), res, I
+
+
+def get_send_disp(np_: int, n: int):
+    s = (C.c_int * np_)()
+    d = (C.c_int * np_)()
+    lib().orc_get_send(np_, n, s)
+    lib().orc_get_disp(np_, n, d)
+    return list(s), list(d)
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
+
+
+# ---------------------------------------------------------------- reference
+_ref = None
+
+
+def ref_lib():
+    """The reference's own functions (None where the reference tree is absent)."""
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            if build_ref() is None:
+                return None
+        L = C.CDLL(str(REF_LIB))
+        L.ref_calculate_int_cpu.restype = C.c_int
+        L.ref_calculate_int_cpu.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_double, _dp, C.c_int, C.c_int, _dp]
+        L.ref_energy_cell.restype = C.c_double
+        L.ref_energy_cell.argtypes = [C.c_int, _dp, _dp, C.c_double, _dp]
+        L.ref_stream_cell.restype = None
+        L.ref_stream_cell.argtypes = [C.c_int, _dp, _dp, C.c_double, _dp, _dp]
+        L.ref_get_send_disp.restype = None
+        L.ref_get_send_disp.argtypes = [C.c_int, C.c_int, _ip, _ip]
+        _ref = L
+    return _ref

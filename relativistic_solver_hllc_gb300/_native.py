@@ -1,0 +1,411 @@
+"""ctypes binding of librts_scatter.so (include/rts_scatter.h).
+
+The product path is the native library; this module only marshals numpy
+arrays into the C ABI.  It never computes anything itself: if the library is
+missing or was built for another machine, loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+from .build import INCLUDE, LIB_PATH
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_CUDA = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_BAD_STATE = 4
+ERR_TIMEOUT = 5
+ERR_OVER_BUDGET = 6
+ERR_UNSUPPORTED = 7
+ERR_DEVICE_WAIT = 8
+
+STATUS_NAMES = {
+    OK: "RTS_OK",
+    ERR_INVALID_ARGUMENT: "RTS_ERR_INVALID_ARGUMENT",
+    ERR_CUDA: "RTS_ERR_CUDA",
+    ERR_OUT_OF_MEMORY: "RTS_ERR_OUT_OF_MEMORY",
+    ERR_BAD_STATE: "RTS_ERR_BAD_STATE",
+    ERR_TIMEOUT: "RTS_ERR_TIMEOUT",
+    ERR_OVER_BUDGET: "RTS_ERR_OVER_BUDGET",
+    ERR_UNSUPPORTED: "RTS_ERR_UNSUPPORTED",
+    ERR_DEVICE_WAIT: "RTS_ERR_DEVICE_WAIT",
+}
+
+STREAM_SCATTERING_1 = 0
+STREAM_SCATTERING_2 = 1
+STREAM_PARAMS = 2
+
+PHASE_THOMSON = 0
+PHASE_HG = 1
+PHASE_CUSTOM = 2
+
+PREC_FP64 = 0
+PREC_BF16X3 = 1
+PREC_FP16X3 = 2
+
+PRECISIONS = {"fp64": PREC_FP64, "bf16x3": PREC_BF16X3, "fp16x3": PREC_FP16X3}
+
+
+class RtsError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str = ""):
+        self.status = status
+        name = STATUS_NAMES.get(status, str(status))
+        super().__init__(f"{where}: {name}" + (f": {message}" if message else ""))
+
+
+_dp = C.POINTER(C.c_double)
+_i64 = C.c_int64
+_vp = C.c_void_p
+
+# name -> (restype, argtypes)
+_SIGNATURES = {
+    "rts_abi_version": (C.c_int, []),
+    "rts_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "rts_ctx_destroy": (C.c_int, [_vp]),
+    "rts_last_error": (C.c_char_p, [_vp]),
+    "rts_set_hbm_budget": (C.c_int, [_vp, _i64]),
+    "rts_hbm_used": (C.c_int, [_vp, C.POINTER(_i64)]),
+    "rts_init": (C.c_int, [_vp, _dp, _dp, _i64, C.c_double, _i64, _i64, _i64]),
+    "rts_host_illum": (C.c_int, [_vp, C.POINTER(_dp)]),
+    "rts_host_scattering": (C.c_int, [_vp, C.POINTER(_dp)]),
+    "rts_set_phase": (C.c_int, [_vp, C.c_int, C.c_double]),
+    "rts_set_weights": (C.c_int, [_vp, _dp]),
+    "rts_send_illum_async": (C.c_int, [_vp, _i64, _i64, _i64, _dp]),
+    "rts_copy_illum": (C.c_int, [_vp, _i64, _dp]),
+    "rts_scattering_async": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
+    "rts_scattering": (C.c_int, [_vp, _dp, _dp]),
+    "rts_read_scattering": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
+    "rts_scattering_update": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_double, _dp]),
+    "rts_device_arrays": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
+    "rts_moments": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "rts_source_update": (C.c_int, [_vp, _dp, C.c_double, _i64, _i64, C.c_int, _dp]),
+    "rts_sync_stream": (C.c_int, [_vp, C.c_int, _i64]),
+    "rts_wait": (C.c_int, [_vp, _i64]),
+    "rts_solve_setup": (C.c_int, [_vp, C.c_int, _dp, C.c_double]),
+    "rts_solve_step": (C.c_int, [_vp, C.c_int, _dp]),
+    "rts_solve_step_async": (C.c_int, [_vp, C.c_int]),
+    "rts_solve_residual": (C.c_int, [_vp, _dp]),
+    "rts_solve_residual_history": (C.c_int, [_vp, _dp, _i64]),
+    "rts_read_illum": (C.c_int, [_vp, _i64, _dp]),
+    "rts_solve_read": (C.c_int, [_vp, _dp]),
+    "rts_solve_read_ibar": (C.c_int, [_vp, _dp]),
+    "rts_synth_illum": (C.c_int, [_vp, C.c_uint64, C.c_double, C.c_double, C.c_int]),
+    "rts_synth_directions": (C.c_int, [_i64, _dp, _dp, _dp]),
+    "rts_synth_uniform": (C.c_int, [C.c_uint64, C.c_uint64, C.c_double, C.c_double, _i64, _i64, _dp]),
+    "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "rts_launch_count": (C.c_int, [_vp, C.POINTER(_i64)]),
+    "rts_kernel_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(_i64)]),
+}
+
+
+def synth_directions(M: int):
+    """Spherical Fibonacci directions (xyz [M][3], area [M], full_area)."""
+    lib = load_library()
+    xyz = np.empty(3 * M)
+    area = np.empty(M)
+    fa = C.c_double()
+    rc = lib.rts_synth_directions(int(M), _ptr(xyz), _ptr(area), C.byref(fa))
+    if rc != OK:
+        raise RtsError(rc, "rts_synth_directions")
+    return xyz.reshape(M, 3), area, fa.value
+
+
+def synth_uniform(seed: int, stream: int, lo: float, hi: float, n: int, i0: int = 0) -> np.ndarray:
+    lib = load_library()
+    out = np.empty(n)
+    rc = lib.rts_synth_uniform(C.c_uint64(seed), C.c_uint64(stream), float(lo), float(hi), int(i0), int(n), _ptr(out))
+    if rc != OK:
+        raise RtsError(rc, "rts_synth_uniform")
+    return out
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Every function the public headers declare (for the export check)."""
+    names = []
+    for h in sorted(Path(INCLUDE).glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        names += re.findall(r"\b(rts_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def load_library(path: str | Path | None = None):
+    """Load librts_scatter.so (built in-tree by build.build_library)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with relativistic_solver_hllc_gb300.build.build_library() "
+            "(there is no CPU fallback)"
+        )
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    arr = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and arr.size != int(np.prod(shape)):
+        raise ValueError(f"expected {int(np.prod(shape))} values, got {arr.size}")
+    return arr
+
+
+class Context:
+    """One device context of the scattering library (one host thread at a time)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = _vp()
+        rc = self.lib.rts_ctx_create(int(device), C.byref(h))
+        if rc != OK:
+            raise RtsError(rc, "rts_ctx_create", f"device {device}")
+        self.h = h
+        self._keep = []  # host arrays referenced by queued async copies
+        self.N = self.M = 0
+        self.start = self.end = 0
+
+    # -- plumbing -------------------------------------------------------
+    def _check(self, rc: int, where: str):
+        if rc != OK:
+            msg = self.lib.rts_last_error(self.h)
+            raise RtsError(rc, where, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rts_ctx_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def last_error(self) -> str:
+        return self.lib.rts_last_error(self.h).decode()
+
+    def set_hbm_budget(self, nbytes: int):
+        self._check(self.lib.rts_set_hbm_budget(self.h, int(nbytes)), "rts_set_hbm_budget")
+
+    def hbm_used(self) -> int:
+        v = _i64()
+        self._check(self.lib.rts_hbm_used(self.h, C.byref(v)), "rts_hbm_used")
+        return v.value
+
+    # -- grid -----------------------------------------------------------
+    def init(self, xyz, area, full_area: float, N: int, start: int = 0, end: int | None = None):
+        xyz = _f64(xyz)
+        area = _f64(area)
+        M = area.size
+        if xyz.size != 3 * M:
+            raise ValueError("xyz must hold 3 values per direction")
+        end = M if end is None else end
+        self._check(
+            self.lib.rts_init(self.h, _ptr(xyz), _ptr(area), M, float(full_area), int(N), int(start), int(end)),
+            "rts_init",
+        )
+        self.N, self.M, self.start, self.end = int(N), int(M), int(start), int(end)
+
+    def host_illum(self) -> np.ndarray:
+        p = _dp()
+        self._check(self.lib.rts_host_illum(self.h, C.byref(p)), "rts_host_illum")
+        return np.ctypeslib.as_array(p, shape=(self.M * self.N * 4,))
+
+    def host_scattering(self) -> np.ndarray:
+        p = _dp()
+        self._check(self.lib.rts_host_scattering(self.h, C.byref(p)), "rts_host_scattering")
+        return np.ctypeslib.as_array(p, shape=((self.end - self.start) * self.N,))
+
+    def set_phase(self, phase: int, g: float = 0.0):
+        self._check(self.lib.rts_set_phase(self.h, int(phase), float(g)), "rts_set_phase")
+
+    def set_weights(self, W):
+        W = _f64(W, (self.M, self.end - self.start))
+        self._check(self.lib.rts_set_weights(self.h, _ptr(W)), "rts_set_weights")
+
+    # -- transfers --------------------------------------------------------
+    def send_illum_async(self, size: int, shift_dev: int, shift_host: int, illum_host: np.ndarray):
+        if illum_host.dtype != np.float64 or not illum_host.flags.c_contiguous:
+            raise ValueError("illum_host must be a C-contiguous float64 array")
+        if shift_host + size > illum_host.size:
+            raise ValueError("host range outside the array")
+        self._keep.append(illum_host)
+        self._check(
+            self.lib.rts_send_illum_async(self.h, int(size), int(shift_dev), int(shift_host), _ptr(illum_host)),
+            "rts_send_illum_async",
+        )
+
+    def copy_illum(self, illum_host, size: int | None = None):
+        a = _f64(illum_host)
+        size = a.size if size is None else size
+        self._check(self.lib.rts_copy_illum(self.h, int(size), _ptr(a)), "rts_copy_illum")
+
+    # -- integrals --------------------------------------------------------
+    def scattering_async(self, start: int, end: int, stream: int, out: np.ndarray | None = None):
+        if out is not None:
+            if out.dtype != np.float64 or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float64 array")
+            if out.size < end * self.N:
+                raise ValueError("out too small for the requested rows")
+            self._keep.append(out)
+        self._check(
+            self.lib.rts_scattering_async(self.h, int(start), int(end), int(stream), _ptr(out)),
+            "rts_scattering_async",
+        )
+
+    def scattering(self, illum=None) -> np.ndarray:
+        out = np.empty((self.end - self.start) * self.N, dtype=np.float64)
+        src = None if illum is None else _f64(illum, (self.M * self.N * 4,))
+        self._check(self.lib.rts_scattering(self.h, _ptr(src), _ptr(out)), "rts_scattering")
+        return out.reshape(self.end - self.start, self.N)
+
+    def moments(self, stream: int = STREAM_PARAMS):
+        e = np.empty(self.N, dtype=np.float64)
+        f = np.empty(self.N * 3, dtype=np.float64)
+        self._check(self.lib.rts_moments(self.h, int(stream), _ptr(e), _ptr(f)), "rts_moments")
+        return e, f.reshape(self.N, 3)
+
+    def source_update(self, B, lam: float, start: int, end: int, stream: int = STREAM_SCATTERING_1,
+                      residual: bool = True):
+        B = _f64(B, (self.N,))
+        r = C.c_double(0.0)
+        self._check(
+            self.lib.rts_source_update(self.h, _ptr(B), float(lam), int(start), int(end), int(stream),
+                                       C.byref(r) if residual else None),
+            "rts_source_update",
+        )
+        return r.value if residual else None
+
+    def scattering_update(self, precision, illum_host: np.ndarray, B: np.ndarray | None, lam: float,
+                          out: np.ndarray) -> np.ndarray:
+        """One evaluation with host buffers (H2D Illum and B, integral + update, D2H S)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        for a in (illum_host, out) + ((B,) if B is not None else ()):
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("host buffers must be C-contiguous float64 arrays")
+        if illum_host.size != self.M * self.N * 4 or out.size != (self.end - self.start) * self.N:
+            raise ValueError("host buffer sizes do not match the grid")
+        self._check(self.lib.rts_scattering_update(self.h, prec, _ptr(illum_host), _ptr(B), float(lam), _ptr(out)),
+                    "rts_scattering_update")
+        return out
+
+    def read_scattering(self, start: int, end: int, stream: int, out: np.ndarray | None = None):
+        if out is not None:
+            if out.dtype != np.float64 or not out.flags.c_contiguous or out.size < end * self.N:
+                raise ValueError("out must be a C-contiguous float64 array covering the rows")
+            self._keep.append(out)
+        self._check(self.lib.rts_read_scattering(self.h, int(start), int(end), int(stream), _ptr(out)),
+                    "rts_read_scattering")
+
+    def device_arrays(self):
+        a, b = _dp(), _dp()
+        self._check(self.lib.rts_device_arrays(self.h, C.byref(a), C.byref(b)), "rts_device_arrays")
+        return C.cast(a, C.c_void_p).value, C.cast(b, C.c_void_p).value
+
+    # -- synchronisation --------------------------------------------------
+    def sync_stream(self, stream: int, timeout_us: int = -1):
+        rc = self.lib.rts_sync_stream(self.h, int(stream), int(timeout_us))
+        if rc == OK:
+            self._keep.clear()
+        self._check(rc, "rts_sync_stream")
+
+    def wait(self, timeout_us: int = -1):
+        rc = self.lib.rts_wait(self.h, int(timeout_us))
+        if rc == OK:
+            self._keep.clear()
+        self._check(rc, "rts_wait")
+
+    # -- resident source iteration ---------------------------------------
+    def solve_setup(self, precision, B, lam: float):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        B = _f64(B, (self.N,))
+        self._check(self.lib.rts_solve_setup(self.h, prec, _ptr(B), float(lam)), "rts_solve_setup")
+
+    def solve_step(self, relax: bool = False) -> float:
+        r = C.c_double(0.0)
+        self._check(self.lib.rts_solve_step(self.h, int(bool(relax)), C.byref(r)), "rts_solve_step")
+        return r.value
+
+    def solve_step_async(self, relax: bool = False):
+        self._check(self.lib.rts_solve_step_async(self.h, int(bool(relax))), "rts_solve_step_async")
+
+    def solve_residual(self) -> float:
+        r = C.c_double(0.0)
+        self._check(self.lib.rts_solve_residual(self.h, C.byref(r)), "rts_solve_residual")
+        return r.value
+
+    def solve_residual_history(self, n: int) -> np.ndarray:
+        out = np.empty(n)
+        self._check(self.lib.rts_solve_residual_history(self.h, _ptr(out), int(n)), "rts_solve_residual_history")
+        return out
+
+    def read_illum(self, out: np.ndarray, size: int | None = None) -> np.ndarray:
+        if out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array")
+        size = out.size if size is None else size
+        self._check(self.lib.rts_read_illum(self.h, int(size), _ptr(out)), "rts_read_illum")
+        return out
+
+    def solve_read(self) -> np.ndarray:
+        out = np.empty(self.M * self.N, dtype=np.float64)
+        self._check(self.lib.rts_solve_read(self.h, _ptr(out)), "rts_solve_read")
+        return out.reshape(self.M, self.N)
+
+    def solve_read_ibar(self) -> np.ndarray:
+        out = np.empty(self.M * self.N, dtype=np.float64)
+        self._check(self.lib.rts_solve_read_ibar(self.h, _ptr(out)), "rts_solve_read_ibar")
+        return out.reshape(self.M, self.N)
+
+    def stream_handle(self, stream: int) -> int:
+        v = _vp()
+        self._check(self.lib.rts_stream_handle(self.h, int(stream), C.byref(v)), "rts_stream_handle")
+        return int(v.value or 0)
+
+    def launch_count(self) -> int:
+        v = _i64()
+        self._check(self.lib.rts_launch_count(self.h, C.byref(v)), "rts_launch_count")
+        return v.value
+
+    def kernel_timing(self, enable: bool):
+        """enable=True clears and starts event timing of the dominant kernel;
+        enable=False stops it and returns (total_ms, launches)."""
+        ms = C.c_double()
+        n = _i64()
+        self._check(self.lib.rts_kernel_timing(self.h, int(bool(enable)), C.byref(ms), C.byref(n)),
+                    "rts_kernel_timing")
+        return ms.value, n.value
+
+    def synth_illum(self, seed: int, mu: float, sigma: float, independent_faces: bool = False):
+        self._check(
+            self.lib.rts_synth_illum(self.h, C.c_uint64(seed), float(mu), float(sigma), int(bool(independent_faces))),
+            "rts_synth_illum",
+        )

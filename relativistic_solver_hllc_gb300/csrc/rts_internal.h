@@ -1,0 +1,142 @@
+// rts_internal.h -- context state and helpers shared by the library's
+// translation units.  Not installed; the public surface is include/rts_scatter.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "rts_scatter.h"
+
+// Error reporting: every entry point returns an rts_status and stores a
+// message in the context.  No path calls exit() (the reference's
+// CUDA_CALL_FUNC exits the process, cuda/cuda_def.cuh:18-20,31-40).
+struct rts_ctx;
+int rts_fail(rts_ctx* ctx, int status, const char* fmt, ...);
+
+#define RTS_CUDA_TRY(ctx, call)                                                            \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return rts_fail((ctx), RTS_ERR_CUDA, "%s failed: %s (%s:%d)", #call,           \
+                            cudaGetErrorString(e_), __FILE__, __LINE__);                   \
+    } while (0)
+
+#define RTS_CHECK_LAUNCH(ctx, what)                                                        \
+    do {                                                                                   \
+        cudaError_t e_ = cudaGetLastError();                                               \
+        if (e_ != cudaSuccess)                                                             \
+            return rts_fail((ctx), RTS_ERR_CUDA, "launch of %s failed: %s", (what),        \
+                            cudaGetErrorString(e_));                                       \
+    } while (0)
+
+#define RTS_REQUIRE(ctx, cond, status, ...)                                                \
+    do {                                                                                   \
+        if (!(cond)) return rts_fail((ctx), (status), __VA_ARGS__);                        \
+    } while (0)
+
+constexpr int64_t RTS_RESID_CAP = 4096;
+
+// Split-precision operands of one source iteration (tensor-core path).
+struct rts_split_state {
+    int precision = -1;
+    int64_t kpad = 0;       // in-direction count padded to the K block
+    int64_t mpad = 0;       // out-direction count padded to the N tile
+    int64_t npad = 0;       // cell count padded to the M tile
+    void* w_hi = nullptr;   // [mpad][kpad] 16-bit, K-major
+    void* w_lo = nullptr;
+    void* i_hi[2] = {nullptr, nullptr};  // [npad][kpad] 16-bit, K-major, ping-pong
+    void* i_lo[2] = {nullptr, nullptr};
+    float* w_colscale = nullptr;   // per out-direction scale folded into W (FP16 mode)
+    float* i_rowscale[2] = {nullptr, nullptr};  // per cell scale of Ibar (FP16 mode)
+    float* s32 = nullptr;   // [M][N] FP32 scattering of the tensor path
+    int cur = 0;            // which ping-pong buffer holds the current Ibar
+    bool s_written = false;
+};
+
+struct rts_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int cc_major = 0, cc_minor = 0;
+    cudaStream_t streams[RTS_STREAM_COUNT] = {nullptr, nullptr, nullptr};
+    std::string last_error;
+
+    int64_t budget_bytes = 0;
+    int64_t used_bytes = 0;
+
+    // directions (grid_directions_t)
+    int64_t M = 0;
+    double full_area = 0.0;
+    std::vector<double> h_xyz, h_area;
+    double* d_xyz = nullptr;   // [M][3]
+    double* d_area = nullptr;  // [M]
+    int phase = RTS_PHASE_THOMSON;
+    double phase_g = 0.0;
+
+    // grid
+    int64_t N = 0;
+    int64_t out_start = 0, out_end = 0;  // local out-directions (InitDevice start/end)
+    double* d_illum = nullptr;   // [M][N][4]
+    double* d_S = nullptr;       // [out_end-out_start][N]
+    double* d_W = nullptr;       // [M][out_end-out_start]
+    double* h_illum = nullptr;   // pinned, [M][N][4]
+    double* h_S = nullptr;       // pinned, [out_end-out_start][N]
+    double* d_energy = nullptr;  // [N]
+    double* d_flux = nullptr;    // [N][3]
+    double* d_B = nullptr;       // [N]
+    // residual bits (non-negative doubles order as u64): slot 0 for
+    // rts_source_update, slots 1..RTS_RESID_CAP a ring of per-step residuals
+    unsigned long long* d_resid = nullptr;
+    unsigned long long* resid_target = nullptr;  // slot the next kernels reduce into
+    int* d_flag = nullptr;       // device-side error flag of bounded waits
+
+    // source iteration
+    int solve_precision = -1;
+    double solve_lambda = 0.0;
+    bool solve_ready = false;
+    bool solve_has_prev = false;
+    int64_t solve_steps = 0;
+    rts_split_state split;
+
+    // instrumentation
+    int64_t launches = 0;        // kernels launched by this context
+    bool timing = false;         // record events around the dominant kernel
+    std::vector<cudaEvent_t> tev;  // pairs (begin, end) of recorded launches
+    size_t tev_used = 0;
+
+    int64_t local() const { return out_end - out_start; }
+};
+
+// Event pair around the dominant kernel when timing is on (no-ops otherwise).
+void rts_timing_begin(rts_ctx* ctx, cudaStream_t st);
+void rts_timing_end(rts_ctx* ctx, cudaStream_t st);
+
+// Device allocation accounted against the context's HBM budget.
+int rts_dmalloc(rts_ctx* ctx, void** p, size_t bytes, const char* what);
+void rts_dfree(rts_ctx* ctx, void* p, size_t bytes);
+
+// Kernel launchers (defined in the .cu files).
+int rts_launch_scatter_fp64(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t st,
+                            const double* B, double lambda, bool update, bool residual);
+int rts_launch_moments(rts_ctx* ctx, cudaStream_t st);
+int rts_launch_update(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t st,
+                      const double* B, double lambda, bool residual);
+int rts_launch_relax_fp64(rts_ctx* ctx, cudaStream_t st);
+int rts_launch_weights(rts_ctx* ctx);
+int rts_launch_synth(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int independent_faces);
+
+// Tensor-core path (rts_split.cu).
+int rts_split_setup(rts_ctx* ctx, int precision);
+int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
+// One evaluation from the device Illum (faces) into the FP64 device S, with
+// the source update when B != nullptr; local out-directions [0, local).
+int rts_split_oneshot(rts_ctx* ctx, int precision, const double* B, double lambda, cudaStream_t st);
+int rts_split_read(rts_ctx* ctx, double* S_host);
+int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host);
+void rts_split_free(rts_ctx* ctx);
+
+// Bytes of one element of the given type, for accounting.
+template <class T>
+inline size_t rts_bytes(int64_t n) { return (size_t)n * sizeof(T); }
