@@ -53,7 +53,9 @@ struct rts_split_state {
     float* i_rowscale[2] = {nullptr, nullptr};  // per cell scale of Ibar (FP16 mode)
     float* s32 = nullptr;   // [M][N] FP32 scattering of the tensor path
     int cur = 0;            // which ping-pong buffer holds the current Ibar
-    bool s_written = false;
+    int bn = 0;             // out-directions per tile
+    // TMA descriptors (CUtensorMap, 128 bytes each): A buffer 0, A buffer 1, W
+    alignas(64) unsigned char maps[3][128] = {};
 };
 
 struct rts_ctx {

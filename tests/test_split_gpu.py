@@ -1,0 +1,127 @@
+"""Parity of the split-precision tensor-core path (tcgen05) with the FP64
+oracle, through the C ABI.
+
+Tolerances (max relative error against FP64, written per precision):
+  fp16x3: 1e-6  (scaled FP16 hi/lo split, three products, FP32 accumulate)
+  bf16x3: 2e-5  (BF16 hi/lo split: 2^-17 per operand, reported, not the headline)
+"""
+import numpy as np
+import pytest
+
+import oracle
+from relativistic_solver_hllc_gb300 import PHASE_HG
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp16x3": 1e-6, "bf16x3": 2e-5}
+# the split of Ibar alone: FP16 hi+lo keeps 22 bits, BF16 hi+lo 16 bits
+SPLIT_TOL = {"fp16x3": 4e-7, "bf16x3": 1.6e-5}
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def problem(N, M, seed=1, sigma=1.5, indep=False):
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(seed, 0.0, sigma, N, M, independent_faces=indep)
+    B = oracle.uniform(seed, 2, 0.1, 1.0, N)
+    return xyz, area, fa, il, B
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+@pytest.mark.parametrize("N,M", [(1000, 64), (333, 17), (700, 200), (260, 300), (128, 1000)])
+def test_single_evaluation(ctx, prec, N, M):
+    xyz, area, fa, il, B = problem(N, M, indep=True)
+    lam = 0.9
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(il)
+    ctx.solve_setup(prec, B, lam)
+    r = ctx.solve_step(False)
+    S = ctx.solve_read()
+    ref = oracle.source_update(oracle.calculate_int_cpu(N, xyz, area, fa, il), B, lam)
+    assert rel_err(S, ref) <= TOL[prec]
+    # first step: residual is max|S - 0|
+    assert abs(r - np.max(np.abs(ref))) <= TOL[prec] * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+def test_split_of_ibar(ctx, prec):
+    N, M = 500, 96
+    xyz, area, fa, il, B = problem(N, M, indep=True)
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(il)
+    ctx.solve_setup(prec, B, 0.5)
+    ib = ctx.solve_read_ibar()
+    assert rel_err(ib, oracle.face_mean(il, N, M)) <= SPLIT_TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+def test_source_iteration_with_relaxation(ctx, prec):
+    N, M, lam, iters = 900, 120, 0.9, 6
+    xyz, area, fa, il, B = problem(N, M)
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(il)
+    ctx.solve_setup(prec, B, lam)
+    res = [ctx.solve_step(True) for _ in range(iters)]
+    S = ctx.solve_read()
+    W = oracle.weights_thomson(xyz, area, fa)
+    S_ref, r_ref, I_ref = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
+    # errors of successive steps compound through a contraction of norm <= 0.95
+    assert rel_err(S, S_ref) <= 4 * TOL[prec]
+    assert rel_err(np.array(res[1:]), r_ref[1:]) <= 1e-2
+    assert rel_err(ctx.solve_read_ibar(), I_ref) <= 4 * TOL[prec]
+    hist = ctx.solve_residual_history(iters)
+    assert np.allclose(hist, res, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+def test_host_buffer_entry_point(ctx, prec):
+    """rts_scattering_update: H2D Illum + B, tensor-core integral + update, D2H S."""
+    N, M, lam = 777, 150, 0.7
+    xyz, area, fa, il, B = problem(N, M, seed=3, indep=True)
+    ctx.init(xyz, area, fa, N)
+    out = np.zeros(M * N)
+    ctx.scattering_update(prec, il, B, lam, out)
+    ref = oracle.source_update(oracle.calculate_int_cpu(N, xyz, area, fa, il), B, lam)
+    assert rel_err(out.reshape(M, N), ref) <= TOL[prec]
+    # lambda = 1: the bare integral (CalculateIntScattering at this precision)
+    ctx.scattering_update(prec, il, None, 1.0, out)
+    assert rel_err(out.reshape(M, N), oracle.calculate_int_cpu(N, xyz, area, fa, il)) <= TOL[prec]
+
+
+def test_shard_of_out_directions_tensor(ctx):
+    N, M = 400, 80
+    xyz, area, fa, il, B = problem(N, M, seed=4)
+    start, end = 13, 61
+    ctx.init(xyz, area, fa, N, start, end)
+    out = np.zeros((end - start) * N)
+    ctx.scattering_update("fp16x3", il, None, 1.0, out)
+    ref = oracle.calculate_int_cpu(N, xyz, area, fa, il, start, end - start)
+    assert rel_err(out.reshape(end - start, N), ref) <= TOL["fp16x3"]
+
+
+def test_hg_phase_tensor(ctx):
+    N, M, g, lam = 600, 146, 0.8, 0.6
+    xyz, area, fa, il, B = problem(N, M, seed=6)
+    ctx.init(xyz, area, fa, N)
+    ctx.set_phase(PHASE_HG, g)
+    ctx.copy_illum(il)
+    ctx.solve_setup("fp16x3", B, lam)
+    ctx.solve_step(False)
+    S = ctx.solve_read()
+    W = oracle.weights_hg(xyz, area, g)
+    ref = oracle.source_update(oracle.scatter_matrix(W, oracle.face_mean(il, N, M)), B, lam)
+    assert rel_err(S, ref) <= TOL["fp16x3"]
+
+
+def test_isotropic_intensity_is_exact_under_hg(ctx):
+    """Known answer: I = c with row-normalised HG weights gives S = c."""
+    N, M, c = 256, 302, 3.25
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    ctx.init(xyz, area, fa, N)
+    ctx.set_phase(PHASE_HG, 0.5)
+    ctx.copy_illum(np.full(M * N * 4, c))
+    ctx.solve_setup("fp16x3", np.ones(N), 1.0)
+    ctx.solve_step(False)
+    S = ctx.solve_read()
+    assert np.max(np.abs(S / c - 1.0)) <= 1e-6
