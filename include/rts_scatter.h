@@ -248,8 +248,38 @@ int rts_synth_uniform(uint64_t seed, uint64_t stream, double lo, double hi, int6
                       double* out);
 
 /* ---------------------------------------------------------------------- */
+/* host formats and partition (no GPU involved)                            */
+/* ---------------------------------------------------------------------- */
+
+/* Direction-set text file of ReadSphereDirectionDecartToSpherical
+ * (file_module/reader_txt.cpp:25-47): M, then M lines "area x y z", then
+ * full_area.  With xyz or area NULL, or capacity < M, only *M is returned. */
+int rts_read_direction_file(const char* path, int64_t capacity, int64_t* M, double* xyz, double* area,
+                            double* full_area);
+int rts_write_direction_file(const char* path, int64_t M, const double* xyz, const double* area,
+                             double full_area);
+
+/* Count-prefixed binary arrays of ReadSimpleFileBin / WriteSimpleFileBin
+ * (file_module/reader_bin.h:13-30, file_module/writer_bin.h:9-26): int32
+ * count, then the raw elements.  With data NULL or capacity < count, only
+ * *count is returned. */
+int rts_read_simple_bin(const char* path, int64_t elem_size, int64_t capacity, void* data, int64_t* count);
+int rts_write_simple_bin(const char* path, int64_t elem_size, int64_t count, const void* data);
+
+/* Out-direction partition over np ranks: GetSend / GetDisp
+ * (solve_module/solve_utils.cpp:177-202). */
+int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
+
+/* ---------------------------------------------------------------------- */
 /* instrumentation                                                         */
 /* ---------------------------------------------------------------------- */
+
+/* Tuning knobs of the tensor-core path (0 restores the default):
+ *   RTS_TUNE_FLUSH: in-direction blocks of 32 accumulated on the tensor core
+ *   before the hi*hi partial sum is added in FP32 on the CUDA cores
+ *   (default 4; smaller is more accurate, larger issues fewer drains). */
+#define RTS_TUNE_FLUSH 1
+int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* The cudaStream_t of a stream slot (for callers that order their own work
  * or record CUDA events against the library's streams). */

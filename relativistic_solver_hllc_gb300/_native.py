@@ -97,6 +97,12 @@ _SIGNATURES = {
     "rts_synth_illum": (C.c_int, [_vp, C.c_uint64, C.c_double, C.c_double, C.c_int]),
     "rts_synth_directions": (C.c_int, [_i64, _dp, _dp, _dp]),
     "rts_synth_uniform": (C.c_int, [C.c_uint64, C.c_uint64, C.c_double, C.c_double, _i64, _i64, _dp]),
+    "rts_read_direction_file": (C.c_int, [C.c_char_p, _i64, C.POINTER(_i64), _dp, _dp, _dp]),
+    "rts_write_direction_file": (C.c_int, [C.c_char_p, _i64, _dp, _dp, C.c_double]),
+    "rts_read_simple_bin": (C.c_int, [C.c_char_p, _i64, _i64, _vp, C.POINTER(_i64)]),
+    "rts_write_simple_bin": (C.c_int, [C.c_char_p, _i64, _i64, _vp]),
+    "rts_partition": (C.c_int, [C.c_int, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
+    "rts_set_tuning": (C.c_int, [_vp, C.c_int, C.c_int]),
     "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "rts_launch_count": (C.c_int, [_vp, C.POINTER(_i64)]),
     "rts_kernel_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(_i64)]),
@@ -113,6 +119,55 @@ def synth_directions(M: int):
     if rc != OK:
         raise RtsError(rc, "rts_synth_directions")
     return xyz.reshape(M, 3), area, fa.value
+
+
+def _status(rc: int, where: str):
+    if rc != OK:
+        raise RtsError(rc, where)
+
+
+def read_direction_file(path):
+    """(xyz [M][3], area [M], full_area) from a direction-set text file."""
+    lib = load_library()
+    M = _i64()
+    _status(lib.rts_read_direction_file(str(path).encode(), 0, C.byref(M), None, None, None), "rts_read_direction_file")
+    xyz = np.empty(3 * M.value)
+    area = np.empty(M.value)
+    fa = C.c_double()
+    _status(lib.rts_read_direction_file(str(path).encode(), M.value, C.byref(M), _ptr(xyz), _ptr(area), C.byref(fa)),
+            "rts_read_direction_file")
+    return xyz.reshape(-1, 3), area, fa.value
+
+
+def write_direction_file(path, xyz, area, full_area: float):
+    xyz = _f64(xyz)
+    area = _f64(area)
+    _status(load_library().rts_write_direction_file(str(path).encode(), area.size, _ptr(xyz), _ptr(area),
+                                                    float(full_area)), "rts_write_direction_file")
+
+
+def read_simple_bin(path, dtype=np.float64) -> np.ndarray:
+    lib = load_library()
+    dt = np.dtype(dtype)
+    n = _i64()
+    _status(lib.rts_read_simple_bin(str(path).encode(), dt.itemsize, 0, None, C.byref(n)), "rts_read_simple_bin")
+    out = np.empty(n.value, dtype=dt)
+    _status(lib.rts_read_simple_bin(str(path).encode(), dt.itemsize, n.value, out.ctypes.data_as(_vp), C.byref(n)),
+            "rts_read_simple_bin")
+    return out
+
+
+def write_simple_bin(path, data: np.ndarray):
+    a = np.ascontiguousarray(data)
+    _status(load_library().rts_write_simple_bin(str(path).encode(), a.dtype.itemsize, a.size, a.ctypes.data_as(_vp)),
+            "rts_write_simple_bin")
+
+
+def partition(np_: int, n: int):
+    s = (C.c_int64 * np_)()
+    d = (C.c_int64 * np_)()
+    _status(load_library().rts_partition(int(np_), int(n), s, d), "rts_partition")
+    return list(s), list(d)
 
 
 def synth_uniform(seed: int, stream: int, lo: float, hi: float, n: int, i0: int = 0) -> np.ndarray:
@@ -384,6 +439,9 @@ class Context:
         out = np.empty(self.M * self.N, dtype=np.float64)
         self._check(self.lib.rts_solve_read_ibar(self.h, _ptr(out)), "rts_solve_read_ibar")
         return out.reshape(self.M, self.N)
+
+    def set_tuning(self, key: int, value: int):
+        self._check(self.lib.rts_set_tuning(self.h, int(key), int(value)), "rts_set_tuning")
 
     def stream_handle(self, stream: int) -> int:
         v = _vp()

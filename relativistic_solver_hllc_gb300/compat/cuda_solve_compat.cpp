@@ -1,0 +1,209 @@
+// cuda_solve_compat.cpp -- the reference's GPU host interface
+// (cuda/cuda_solve.h:5-37) implemented over the C ABI of librts_scatter.so.
+//
+// Drop-in use: compile this file into the reference's solver in place of
+// cuda/cuda_solve.cu and cuda/cuda_struct.cu (with USE_CUDA defined, so that
+// the reference's cuda/cuda_solve.h and solve_module/solve_global_struct.h
+// provide grid_t, grid_directions_t and e_cuda_stream_id_t) and link
+// librts_scatter.so.  The caller -- MPI_CalculateIllumAsync
+// (solve_module/illum/Illum_async.cpp:616-1097), CalculateIllumParam (:1390),
+// RunSolveModule (solve_module/solve_main.cpp:135-136,315) -- is unchanged.
+//
+// Behaviour kept from the reference: one process-wide device context created
+// by SetDevice; InitDevice hands pinned host arrays to grid_t (Illum,
+// scattering, and on the first rank the moment arrays); the Illum copies go on
+// stream eCuda_scattering_1; every function returns 0 on success.
+// Behaviour changed on purpose: errors are printed and reported with a return
+// value of 1 (or, for void functions, remembered and printed) instead of
+// exit(1) (cuda/cuda_def.cuh:14-20); the D2H of
+// CalculateIntScatteringAsyncMPIStream lands at row `start` (start*N
+// elements), where the reference offsets by `start` elements
+// (cuda/cuda_solve.cu:107), which is the same for the start == 0 the solver
+// uses; CalculateEnergy / CalculateStream compute the moments (their kernels
+// are commented out in the reference, cuda/cuda_solve.cu:182,236,259).
+#include <cstdio>
+#include <vector>
+
+#include "cuda_solve.h"
+#include "rts_scatter.h"
+
+namespace {
+
+rts_ctx* g_ctx = nullptr;
+int g_device = 0;
+bool g_owns_moments = false;
+
+int report(int rc, const char* where)
+{
+    if (rc != RTS_OK)
+        std::fprintf(stderr, "%s failed: status %d: %s\n", where, rc, g_ctx ? rts_last_error(g_ctx) : "");
+    return rc == RTS_OK ? 0 : 1;
+}
+
+rts_stream_id stream_of(e_cuda_stream_id_t s)
+{
+    switch (s) {
+    case eCuda_scattering_1: return RTS_STREAM_SCATTERING_1;
+    case eCuda_scattering_2: return RTS_STREAM_SCATTERING_2;
+    default: return RTS_STREAM_PARAMS;
+    }
+}
+
+}  // namespace
+
+void SetDevice(const int num_dev)
+{
+    if (g_ctx) rts_ctx_destroy(g_ctx);
+    g_ctx = nullptr;
+    g_device = num_dev;
+    report(rts_ctx_create(num_dev, &g_ctx), "SetDevice");
+}
+
+void InitDevice(const grid_directions_t& grid_dir_host, grid_t& grid_host, const int start, const int end)
+{
+    if (!g_ctx) SetDevice(g_device);
+    if (!g_ctx) return;
+    const int M = grid_dir_host.size;
+    std::vector<double> xyz(3 * (size_t)M), area((size_t)M);
+    for (int i = 0; i < M; ++i) {
+        xyz[3 * i + 0] = grid_dir_host.directions[i].dir[0];
+        xyz[3 * i + 1] = grid_dir_host.directions[i].dir[1];
+        xyz[3 * i + 2] = grid_dir_host.directions[i].dir[2];
+        area[i] = grid_dir_host.directions[i].area;
+    }
+    if (report(rts_init(g_ctx, xyz.data(), area.data(), M, grid_dir_host.full_area, grid_host.size, start, end),
+               "InitDevice"))
+        return;
+    rts_host_illum(g_ctx, &grid_host.Illum);
+    rts_host_scattering(g_ctx, &grid_host.scattering);
+    if (start == 0) {  // the first rank also receives the moments (cuda/cuda_struct.cu:158-175)
+        grid_host.divstream = new Type[grid_host.size]();
+        grid_host.divimpuls = new Vector3[grid_host.size]();
+        grid_host.energy = new Type[grid_host.size]();
+        grid_host.stream = new Vector3[grid_host.size]();
+        grid_host.impuls = new Matrix3[grid_host.size]();
+        g_owns_moments = true;
+    }
+}
+
+void ClearDevice()
+{
+    rts_ctx_destroy(g_ctx);  // frees the pinned Illum / scattering too
+    g_ctx = nullptr;
+}
+
+void ClearHost(grid_t& grid_host)
+{
+    // Illum and scattering belong to the context (freed by ClearDevice)
+    grid_host.Illum = nullptr;
+    grid_host.scattering = nullptr;
+    if (g_owns_moments) {
+        delete[] grid_host.divstream;
+        delete[] grid_host.divimpuls;
+        delete[] grid_host.energy;
+        delete[] grid_host.stream;
+        delete[] grid_host.impuls;
+        g_owns_moments = false;
+    }
+    grid_host.divstream = nullptr;
+    grid_host.divimpuls = nullptr;
+    grid_host.energy = nullptr;
+    grid_host.stream = nullptr;
+    grid_host.impuls = nullptr;
+}
+
+void CudaWait() { report(rts_wait(g_ctx, -1), "CudaWait"); }
+
+void CudaSyncStream(const e_cuda_stream_id_t stream_id)
+{
+    report(rts_sync_stream(g_ctx, stream_of(stream_id), -1), "CudaSyncStream");
+}
+
+void CudaEventPrint()
+{
+    double ms = 0.0;
+    int64_t n = 0;
+    if (rts_kernel_timing(g_ctx, 0, &ms, &n) == RTS_OK && n > 0)
+        std::printf("scattering kernels: %lld launches, %f ms total\n", (long long)n, ms);
+    rts_kernel_timing(g_ctx, 1, nullptr, nullptr);
+}
+
+void CudaSendIllumAsync(const int size, const int shift, const Type* Illum_host)
+{
+    report(rts_send_illum_async(g_ctx, size, shift, shift, Illum_host), "CudaSendIllumAsync");
+}
+
+void CudaSendIllumAsync(const int size, const int shift_dev, const int shift_host, const Type* Illum_host)
+{
+    report(rts_send_illum_async(g_ctx, size, shift_dev, shift_host, Illum_host), "CudaSendIllumAsync");
+}
+
+void CopyIllumOnDevice(const int size, const Type* Illum_host)
+{
+    report(rts_copy_illum(g_ctx, size, Illum_host), "CopyIllumOnDevice");
+}
+
+int CalculateIntScatteringAsyncMPIStream(const grid_directions_t&, grid_t& grid, const int start, const int end,
+                                         const e_cuda_stream_id_t stream)
+{
+    return report(rts_scattering_async(g_ctx, start, end, stream_of(stream), grid.scattering),
+                  "CalculateIntScatteringAsyncMPIStream");
+}
+
+int CalculateIntScatteringAsyncMPI(const grid_directions_t&, grid_t& grid, int local_size)
+{
+    return report(rts_scattering_async(g_ctx, 0, local_size, RTS_STREAM_SCATTERING_1, grid.scattering),
+                  "CalculateIntScatteringAsyncMPI");
+}
+
+int CalculateIntScatteringAsync(const grid_directions_t& grid_dir, grid_t& grid)
+{
+    return report(rts_scattering_async(g_ctx, 0, grid_dir.size, RTS_STREAM_SCATTERING_1, grid.scattering),
+                  "CalculateIntScatteringAsync");
+}
+
+int CalculateIntScattering(const grid_directions_t&, grid_t& grid)
+{
+    return report(rts_scattering(g_ctx, grid.Illum, grid.scattering), "CalculateIntScattering");
+}
+
+int CalculateEnergy(const grid_directions_t&, grid_t& grid)
+{
+    return report(rts_moments(g_ctx, RTS_STREAM_PARAMS, grid.energy, nullptr), "CalculateEnergy");
+}
+
+int CalculateStream(const grid_directions_t&, grid_t& grid)
+{
+    return report(rts_moments(g_ctx, RTS_STREAM_PARAMS, nullptr, reinterpret_cast<double*>(grid.stream)),
+                  "CalculateStream");
+}
+
+int CalculateImpuls(const grid_directions_t&, grid_t&)
+{
+    std::fprintf(stderr, "CalculateImpuls: the pressure-tensor moment is not provided by librts_scatter\n");
+    return 1;
+}
+
+int CalculateDivImpuls(const grid_directions_t&, grid_t&)
+{
+    std::fprintf(stderr, "CalculateDivImpuls: divergence moments are not provided by librts_scatter\n");
+    return 1;
+}
+
+int CalculateDivStream(const grid_directions_t&, grid_t&)
+{
+    std::fprintf(stderr, "CalculateDivStream: divergence moments are not provided by librts_scatter\n");
+    return 1;
+}
+
+int CalculateAllParam(const grid_directions_t& grid_dir, grid_t& grid)
+{
+    return CalculateAllParamStream(grid_dir, grid, eCuda_params);
+}
+
+int CalculateAllParamStream(const grid_directions_t&, grid_t& grid, e_cuda_stream_id_t st)
+{
+    // energy and flux (stream); the divergence moments need the cell geometry
+    return report(rts_moments(g_ctx, stream_of(st), grid.energy, reinterpret_cast<double*>(grid.stream)),
+                  "CalculateAllParamStream");
+}

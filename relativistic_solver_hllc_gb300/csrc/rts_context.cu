@@ -687,6 +687,20 @@ int rts_synth_illum(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int in
     return rts_launch_synth(ctx, seed, mu, sigma, independent_faces);
 }
 
+int rts_set_tuning(rts_ctx* ctx, int key, int value)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    switch (key) {
+    case RTS_TUNE_FLUSH:
+        RTS_REQUIRE(ctx, value >= 0 && value <= 1024, RTS_ERR_INVALID_ARGUMENT,
+                    "flush period %d outside [0, 1024]", value);
+        ctx->split_flush = value;
+        return RTS_OK;
+    default:
+        return rts_fail(ctx, RTS_ERR_INVALID_ARGUMENT, "unknown tuning key %d", key);
+    }
+}
+
 int rts_stream_handle(rts_ctx* ctx, int stream, void** handle)
 {
     if (!ctx || !handle) return RTS_ERR_INVALID_ARGUMENT;

@@ -101,6 +101,7 @@ struct rts_ctx {
     bool solve_has_prev = false;
     int64_t solve_steps = 0;
     rts_split_state split;
+    int split_flush = 0;         // hi*hi drain period in stages (0: default)
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context

@@ -15,16 +15,14 @@
 // into shared memory and the three products address them at byte offsets 0 /
 // 64 inside the same swizzle atom.
 //
-// Kernel: one CTA per 128-cell x BN-out-direction tile (BN <= 256), 192
-// threads: warp 0 issues TMA loads into a 2-stage ring, warp 1 owns the TMEM
-// accumulator (256 columns) and issues tcgen05.mma from one thread, warps 2-5
-// drain TMEM (tcgen05.ld 32x32b) and run the fused epilogue: unscaling, the
-// source update (1-lambda) B + lambda S, the residual max|S - S_prev|, the
-// store of S and, in the source iteration, the relaxation
-// Ibar <- 0.5 Ibar + 0.5 S written back in split form for the next step.
-// Shared memory (~97 KB) allows two CTAs per SM, so one CTA's epilogue
-// overlaps the other's main loop; the two accumulators fill the 512 TMEM
-// columns exactly.  Every mbarrier wait is bounded (2 s of %globaltimer);
+// Kernel (rts_split_gemm.cuh): one CTA per 128-cell x BN-out-direction tile
+// (BN <= 256), 320 threads: warp 0 issues TMA loads into a 4-stage ring,
+// warp 1 owns TMEM (hi*hi and cross-term accumulators) and issues tcgen05.mma
+// from one thread, warps 2-9 drain TMEM (tcgen05.ld 32x32b) and run the fused
+// epilogue: unscaling, the source update (1-lambda) B + lambda S, the residual
+// max|S - S_prev|, the store of S and, in the source iteration, the
+// relaxation Ibar <- 0.5 Ibar + 0.5 S written back in split form for the next
+// step.  Every mbarrier wait is bounded (2 s of %globaltimer);
 // a wait that gives up sets the context's device flag and the kernel drains
 // and exits instead of hanging.
 //
@@ -46,13 +44,10 @@ namespace {
 constexpr int BM = 128;            // cells per tile (UMMA M, TMEM lanes)
 constexpr int KS = 32;             // in-directions per stage (64 halves per row)
 constexpr int MAX_BN = 256;        // out-directions per tile (UMMA N)
-constexpr int STAGES = 2;
 constexpr int A_BYTES = BM * 128;
 constexpr int B_BYTES = MAX_BN * 128;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int GEMM_THREADS = 192;
-constexpr uint32_t TMEM_COLS = 256;
-constexpr size_t GEMM_SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int DEFAULT_FLUSH = 4;   // stages (x32 in-directions) per hi*hi drain
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 
 enum { MODE_ITER = 0, MODE_ONESHOT = 1 };
@@ -374,196 +369,7 @@ __global__ void s32_to_f64_kernel(const float* __restrict__ s, double* __restric
 }
 
 // ------------------------------------------------------------------ GEMM
-struct GemmArgs {
-    int64_t N;        // cells
-    int Mout;         // valid out-directions (columns of D)
-    int kblocks;      // kpad / 32
-    int kpad;
-    int bn;           // columns per tile
-    int n_tiles;
-    uint32_t idesc;
-    const float* rs_inv;  // [npad] or null (BF16)
-    const float* rs;
-    const float* cs_inv;  // [mpad] or null
-    const double* B;      // [N] or null (no update)
-    float lam;
-    float* S32;           // MODE_ITER: [Mout][N]
-    double* S64;          // MODE_ONESHOT: [Mout][N]
-    const uint16_t* a_cur;
-    uint16_t* a_next;     // relaxation target (MODE_ITER, relax)
-    int relax;
-    int residual;
-    unsigned long long* resid;
-    int* flag;
-};
-
-template <bool kFp16, int kMode>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
-split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  const GemmArgs args)
-{
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
-    const uint32_t smem_base = smem_u32(smem);
-    const uint32_t bar_base = smem_u32(bars);
-    auto full_bar = [&](int s) { return bar_base + 8u * s; };
-    auto empty_bar = [&](int s) { return bar_base + 8u * (STAGES + s); };
-    const uint32_t tmem_full_bar = bar_base + 8u * (2 * STAGES);
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_tile = blockIdx.x % args.n_tiles;
-    const int64_t m_tile = blockIdx.x / args.n_tiles;
-    const int bn = args.bn;
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(full_bar(s), 1);
-            mbar_init(empty_bar(s), 1);
-        }
-        mbar_init(tmem_full_bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    const bool live = *(volatile int*)args.flag == 0;
-
-    if (warp == 0) {
-        if (lane == 0 && live) {
-            // ---------------- TMA producer
-            const uint32_t tx = (uint32_t)(A_BYTES + bn * 128);
-            int kb = 0;
-            for (; kb < args.kblocks; ++kb) {
-                const int s = kb % STAGES;
-                if (kb >= STAGES && !mbar_wait(empty_bar(s), ((kb / STAGES) - 1) & 1, args.flag, FLAG_WAIT_PRODUCER))
-                    break;
-                mbar_expect_tx(full_bar(s), tx);
-                const uint32_t sa = smem_base + s * STAGE_BYTES;
-                tma_load_2d(sa, &tmA, kb * 64, (int)(m_tile * BM), full_bar(s));
-                tma_load_2d(sa + A_BYTES, &tmB, kb * 64, n_tile * bn, full_bar(s));
-            }
-            // drain: no copy may still be in flight when the CTA exits
-            for (int i = (kb > STAGES ? kb - STAGES : 0); i < kb; ++i)
-                mbar_wait(full_bar(i % STAGES), (i / STAGES) & 1, args.flag, FLAG_WAIT_PRODUCER);
-        }
-    } else if (warp == 1) {
-        if (lane == 0 && live) {
-            // ---------------- MMA issuer
-            for (int kb = 0; kb < args.kblocks; ++kb) {
-                const int s = kb % STAGES;
-                if (!mbar_wait(full_bar(s), (kb / STAGES) & 1, args.flag, FLAG_WAIT_MMA)) break;
-                tc_fence_after();
-                const uint32_t sa = smem_base + s * STAGE_BYTES;
-                const uint64_t ad = smem_desc_sw128(sa);
-                const uint64_t bd = smem_desc_sw128(sa + A_BYTES);
-#pragma unroll
-                for (int ks = 0; ks < 2; ++ks) {
-                    const uint64_t hi = (uint64_t)((32 * ks) >> 4);
-                    const uint64_t lo = (uint64_t)((64 + 32 * ks) >> 4);
-                    umma_f16(tmem, ad + hi, bd + hi, args.idesc, (kb | ks) != 0);
-                    umma_f16(tmem, ad + hi, bd + lo, args.idesc, 1u);
-                    umma_f16(tmem, ad + lo, bd + hi, args.idesc, 1u);
-                }
-                umma_commit(empty_bar(s));
-            }
-            umma_commit(tmem_full_bar);  // also after a failed wait: drains issued MMAs
-        }
-    } else {
-        // ---------------- epilogue: warps 2..5, TMEM lane quarter = warp % 4
-        const int q = warp & 3;
-        const int64_t c = m_tile * BM + q * 32 + lane;
-        bool ok = true;
-        if (lane == 0) ok = mbar_wait(tmem_full_bar, 0, args.flag, FLAG_WAIT_EPILOGUE);
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-        __syncwarp();
-        tc_fence_after();
-        if (ok && live) {
-            const bool in_row = c < args.N;
-            const float rinv = (kFp16 && in_row) ? args.rs_inv[c] : 1.0f;
-            const float rsc = (kFp16 && in_row) ? args.rs[c] : 1.0f;
-            const float bterm = (args.B && in_row) ? (float)((1.0 - (double)args.lam) * args.B[c]) : 0.0f;
-            const float lam = args.B ? args.lam : 1.0f;
-            float rmax = 0.0f;
-            bool overflow = false;
-            const int chunks = bn / 16;
-            for (int ch = 0; ch < chunks; ++ch) {
-                float v[16];
-                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 16), v);
-                const int k0 = n_tile * bn + ch * 16;
-                if (!in_row || k0 >= args.Mout) continue;
-                if (kMode == MODE_ITER) {
-                    uint16_t nh[16], nl[16];
-                    uint4 ch_hi[2], ch_lo[2];
-                    const bool do_relax = args.relax && k0 < args.kpad;
-                    if (do_relax) {
-                        const uint4* src = reinterpret_cast<const uint4*>(args.a_cur + c * 2 * (int64_t)args.kpad + ilv_hi(k0));
-                        ch_hi[0] = src[0];
-                        ch_hi[1] = src[1];
-                        ch_lo[0] = src[4];
-                        ch_lo[1] = src[5];
-                    }
-                    const uint16_t* ph = reinterpret_cast<const uint16_t*>(ch_hi);
-                    const uint16_t* pl = reinterpret_cast<const uint16_t*>(ch_lo);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int k = k0 + i;
-                        float xnext = 0.0f;
-                        if (k < args.Mout) {
-                            const float cinv = kFp16 ? __ldg(args.cs_inv + k) : 1.0f;
-                            const float sint = v[i] * rinv * cinv;
-                            const float snew = bterm + lam * sint;
-                            float* dst = args.S32 + (int64_t)k * args.N + c;
-                            if (args.residual) rmax = fmaxf(rmax, fabsf(snew - *dst));
-                            *dst = snew;
-                            if (do_relax) xnext = 0.5f * Split<kFp16>::join(ph[i], pl[i]) + 0.5f * (snew * rsc);
-                        }
-                        if (do_relax) {
-                            if (kFp16 && fabsf(xnext) > 60000.0f) overflow = true;
-                            Split<kFp16>::run(xnext, nh[i], nl[i]);
-                        }
-                    }
-                    if (do_relax) {
-                        uint4* dst = reinterpret_cast<uint4*>(args.a_next + c * 2 * (int64_t)args.kpad + ilv_hi(k0));
-                        const uint32_t* h32 = reinterpret_cast<const uint32_t*>(nh);
-                        const uint32_t* l32 = reinterpret_cast<const uint32_t*>(nl);
-                        dst[0] = make_uint4(h32[0], h32[1], h32[2], h32[3]);
-                        dst[1] = make_uint4(h32[4], h32[5], h32[6], h32[7]);
-                        dst[4] = make_uint4(l32[0], l32[1], l32[2], l32[3]);
-                        dst[5] = make_uint4(l32[4], l32[5], l32[6], l32[7]);
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int k = k0 + i;
-                        if (k < args.Mout) {
-                            const float cinv = kFp16 ? __ldg(args.cs_inv + k) : 1.0f;
-                            const float sint = v[i] * rinv * cinv;
-                            args.S64[(int64_t)k * args.N + c] = (double)(bterm + lam * sint);
-                        }
-                    }
-                }
-            }
-            if (overflow) atomicOr(args.flag, FLAG_SCALE_OVERFLOW);
-            if (kMode == MODE_ITER && args.residual) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-                if (lane == 0 && rmax > 0.0f)
-                    atomicMax(args.resid, (unsigned long long)__double_as_longlong((double)rmax));
-            }
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 1) {
-        tc_fence_after();
-        tmem_dealloc(tmem, TMEM_COLS);
-    }
-}
+#include "rts_split_gemm.cuh"
 
 // ------------------------------------------------------------------ host side
 PFN_cuTensorMapEncodeTiled_v12000 get_encode(rts_ctx* ctx)
@@ -627,11 +433,11 @@ int launch_gemm(rts_ctx* ctx, const CUtensorMap& mA, const CUtensorMap& mB, cons
                 int64_t m_tiles, cudaStream_t st)
 {
     auto kern = split_gemm_kernel<kFp16, kMode>;
-    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM));
+    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM2));
     const int64_t grid = m_tiles * a.n_tiles;
     RTS_REQUIRE(ctx, grid < (1ll << 31), RTS_ERR_UNSUPPORTED, "tensor-path grid too large");
     rts_timing_begin(ctx, st);
-    kern<<<(unsigned)grid, GEMM_THREADS, GEMM_SMEM, st>>>(mA, mB, a);
+    kern<<<(unsigned)grid, GEMM_THREADS2, GEMM_SMEM2, st>>>(mA, mB, a);
     rts_timing_end(ctx, st);
     RTS_CHECK_LAUNCH(ctx, "split_gemm_kernel");
     ctx->launches++;
@@ -742,6 +548,7 @@ GemmArgs base_args(rts_ctx* ctx, bool fp16)
     a.bn = sp.bn;
     a.n_tiles = (int)(sp.mpad / a.bn);
     a.idesc = make_idesc(fp16, a.bn);
+    a.flush = ctx->split_flush > 0 ? ctx->split_flush : DEFAULT_FLUSH;
     a.rs = fp16 ? sp.i_rowscale[0] : nullptr;
     a.rs_inv = fp16 ? rowscale_inv(ctx) : nullptr;
     a.cs_inv = fp16 ? colscale_inv(ctx) : nullptr;

@@ -1,0 +1,53 @@
+"""The reference-named host interface (cuda_solve_compat.cpp) driven in the
+reference's calling order by a C++ program, compared with the oracle."""
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT
+from relativistic_solver_hllc_gb300 import _native
+
+COMPAT = ROOT / "relativistic_solver_hllc_gb300" / "compat"
+
+
+def build_driver(out_dir):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    exe = out_dir / "compat_driver"
+    lib_dir = _native.LIB_PATH.parent
+    cmd = [gxx, "-O2", "-std=c++17", f"-I{COMPAT / 'standin'}", f"-I{ROOT / 'include'}",
+           str(COMPAT / "cuda_solve_compat.cpp"), str(ROOT / "tests" / "compat" / "compat_driver.cpp"),
+           f"-L{lib_dir}", "-lrts_scatter", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_compat_shim_compiles_against_standin(native_lib, tmp_path):
+    """CPU check: the shim and the driver compile and link against the library."""
+    assert build_driver(tmp_path).exists()
+
+
+@pytest.mark.gpu
+def test_reference_calling_sequence(native_lib, tmp_path):
+    exe = build_driver(tmp_path)
+    N, M = 1500, 48
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(12, 0.0, 1.0, N, M, independent_faces=True)
+    _native.write_direction_file(tmp_path / "dirs.txt", xyz, area, fa)
+    _native.write_simple_bin(tmp_path / "Illum.bin", il)
+    res = subprocess.run([str(exe), str(tmp_path / "dirs.txt"), str(tmp_path / "Illum.bin"), str(N), str(tmp_path)],
+                         capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr
+    ref = oracle.calculate_int_cpu(N, xyz, area, fa, il)
+    for name in ("scattering.bin", "scattering_sync.bin"):
+        S = _native.read_simple_bin(tmp_path / name).reshape(M, N)
+        assert float(np.max(np.abs(S - ref) / ref)) <= 1e-12
+    e = _native.read_simple_bin(tmp_path / "energy.bin")
+    assert float(np.max(np.abs(e - oracle.energy(il, N, area, fa)) / e)) <= 1e-12
+    dt = np.dtype([("v", np.float64, 3)])
+    s = _native.read_simple_bin(tmp_path / "stream.bin", dt)["v"]
+    assert float(np.max(np.abs(s - oracle.stream(il, N, xyz, area, fa)) / e[:, None])) <= 1e-12
