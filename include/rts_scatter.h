@@ -277,7 +277,7 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
 /* Tuning knobs of the tensor-core path (0 restores the default):
  *   RTS_TUNE_FLUSH: in-direction blocks of 32 accumulated on the tensor core
  *   before the hi*hi partial sum is added in FP32 on the CUDA cores
- *   (default 4; smaller is more accurate, larger issues fewer drains). */
+ *   (default 1; smaller is more accurate, larger issues fewer drains). */
 #define RTS_TUNE_FLUSH 1
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 

@@ -47,7 +47,7 @@ constexpr int MAX_BN = 256;        // out-directions per tile (UMMA N)
 constexpr int A_BYTES = BM * 128;
 constexpr int B_BYTES = MAX_BN * 128;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int DEFAULT_FLUSH = 4;   // stages (x32 in-directions) per hi*hi drain
+constexpr int DEFAULT_FLUSH = 1;   // stages (x32 in-directions) per hi*hi drain
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 
 enum { MODE_ITER = 0, MODE_ONESHOT = 1 };
