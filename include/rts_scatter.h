@@ -161,6 +161,27 @@ int rts_read_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, do
 int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
                           const double* B_host, double lambda, double* S_host);
 
+/* Allocation-free FP64 scattering integral.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory --
+ * code that runs inside a caller-owned memory pool or arena, code called
+ * while a stream is being captured into a CUDA graph (a cudaMalloc there would
+ * break the capture), and hosts that budget every device byte up front.
+ * The caller passes device pointers: Illum [M][N][4], directions xyz [M][3]
+ * and area [M], and the output scattering [M][N] (all out-directions); the
+ * work is queued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and nothing is synchronised or allocated -- no cudaMalloc, cudaFree or
+ * allocating library call.  The only scratch, the M x M FP64 direction-pair
+ * matrix, lives in a fixed 2 MB device array of the library that every GPU
+ * loading the library holds until the process exits; hence the limit
+ * M <= RTS_NOALLOC_MAX_DIRS (larger M returns RTS_ERR_INVALID_ARGUMENT).
+ * The scratch is shared by all calls and rewritten in full by each: calls
+ * that overlap on the GPU race.  The first call on a device looks the scratch
+ * address up for that device (cudaGetSymbolAddress, with that device
+ * current); make that first call before any stream capture. */
+#define RTS_NOALLOC_MAX_DIRS 512
+int rts_scattering_noalloc(const double* d_illum, const double* d_xyz, const double* d_area, int64_t N,
+                           int64_t M, double full_area, double* d_scattering, void* stream);
+
 /* Device pointers of the resident arrays (for callers that keep data on the
  * GPU): Illum [M][N][4] and scattering [end-start][N]. */
 int rts_device_arrays(rts_ctx* ctx, double** d_illum, double** d_scattering);

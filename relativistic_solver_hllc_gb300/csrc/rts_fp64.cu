@@ -19,6 +19,7 @@
 // at a small fraction of its FP32 rate, so this kernel is FP64-pipe bound by
 // design; memory traffic is ~40 B per cell-direction pair over M in-directions.
 #include <cstdint>
+#include <mutex>
 
 #include "rts_internal.h"
 
@@ -395,5 +396,73 @@ int rts_launch_synth(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int i
     RTS_CHECK_LAUNCH(ctx, "synth_illum_kernel");
     ctx->launches++;
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->streams[RTS_STREAM_SCATTERING_1]));
+    return RTS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free FP64 scattering integral.
+//
+// For callers that cannot allocate device memory themselves or through us:
+// code running under a caller-owned memory pool or arena that forbids
+// allocations outside it, code called while a stream is being captured
+// (where cudaMalloc would break the capture), and hosts that account every
+// device byte up front.  The caller passes device inputs and outputs; the only
+// scratch -- the M x M FP64 direction-pair matrix W -- lives in the
+// file-scope array below, which every GPU that loads this library holds
+// until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+static __device__ __align__(256) double g_noalloc_w[RTS_NOALLOC_MAX_DIRS * RTS_NOALLOC_MAX_DIRS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+double* g_noalloc_w_addr[NOALLOC_MAX_DEVICES] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array, looked up once per device with that
+// device current (host code cannot use the symbol itself as a pointer).
+double* noalloc_scratch(int device)
+{
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_w_addr[device]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_w) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_noalloc_w_addr[device] = static_cast<double*>(p);
+    }
+    return g_noalloc_w_addr[device];
+}
+
+}  // namespace
+
+extern "C" int rts_scattering_noalloc(const double* d_illum, const double* d_xyz, const double* d_area,
+                                      int64_t N, int64_t M, double full_area, double* d_scattering,
+                                      void* stream)
+{
+    if (!d_illum || !d_xyz || !d_area || !d_scattering) return RTS_ERR_INVALID_ARGUMENT;
+    if (N <= 0 || M <= 0 || !(full_area > 0.0)) return RTS_ERR_INVALID_ARGUMENT;
+    if (M > RTS_NOALLOC_MAX_DIRS) return RTS_ERR_INVALID_ARGUMENT;  // the scratch holds M <= 512
+    const int64_t gx = (N + F64_TC - 1) / F64_TC;
+    if (gx >= (1ll << 31)) return RTS_ERR_INVALID_ARGUMENT;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return RTS_ERR_CUDA;
+    }
+    double* W = noalloc_scratch(device);
+    if (!W) return RTS_ERR_CUDA;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // W is rewritten in full (all M x M entries) by every call: nothing in the
+    // scratch has to start at zero, and calls that overlap on the GPU race.
+    weights_kernel<<<(unsigned)((M + 127) / 128), 128, 0, st>>>(d_xyz, d_area, (int)M, 0, (int)M, full_area,
+                                                                RTS_PHASE_THOMSON, 0.0, W);
+    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
+    dim3 grid((unsigned)gx, (unsigned)((M + F64_TK - 1) / F64_TK));
+    scatter_fp64_kernel<false, false><<<grid, F64_THREADS, 0, st>>>(d_illum, W, N, (int)M, (int)M, 0, (int)M,
+                                                                     d_scattering, nullptr, 0.0, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
     return RTS_OK;
 }

@@ -1,0 +1,69 @@
+"""The allocation-free entry point rts_scattering_noalloc.
+
+Callers that cannot allocate device memory -- code inside a caller-owned
+memory pool, code running while a stream is captured into a CUDA graph, hosts
+that budget every device byte -- pass their own device buffers; the library's
+only scratch is a fixed device array.  This test calls the entry point through
+the C ABI twice in a row, with different problem sizes, and checks each result
+against the context-based entry point rts_scattering on the same inputs,
+within the FP64 tolerance of the other parity tests (1e-12 relative).
+
+Kept in a file of its own, collected last, so that a run that stops at the
+first failure has run every other test first.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from relativistic_solver_hllc_gb300 import Context, _native
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to("cuda")
+
+
+def _call_noalloc(lib, torch, il, xyz, area, fa, N, M):
+    d_il, d_xyz, d_area = _dev(torch, il), _dev(torch, xyz), _dev(torch, area)
+    d_S = torch.full((M * N,), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    fn = lib.rts_scattering_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
+    rc = fn(d_il.data_ptr(), d_xyz.data_ptr(), d_area.data_ptr(), N, M, fa, d_S.data_ptr(), stream)
+    assert rc == _native.OK
+    torch.cuda.synchronize()
+    return d_S.cpu().numpy().reshape(M, N)
+
+
+def test_noalloc_matches_context_entry_point(native_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    lib = native_lib
+    with Context(0) as ctx:
+        for N, M, seed in ((3000, 200, 21), (1717, 37, 22)):
+            xyz, area, fa = oracle.fibonacci_directions(M)
+            il = oracle.illum(seed, 0.0, 1.5, N, M, independent_faces=True)
+            S_noalloc = _call_noalloc(lib, torch, il, xyz, area, fa, N, M)
+            ctx.init(xyz, area, fa, N)
+            S_ctx = ctx.scattering(il)
+            err = float(np.max(np.abs(S_noalloc - S_ctx) / np.abs(S_ctx)))
+            assert err <= TOL, (N, M, err)
+
+
+def test_noalloc_rejects_oversized_direction_sets(native_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    fn = native_lib.rts_scattering_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    p = buf.data_ptr()
+    assert fn(p, p, p, 1, 513, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
+    assert fn(None, p, p, 1, 4, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
