@@ -251,6 +251,91 @@ int rts_read_illum(rts_ctx* ctx, int64_t size, double* illum_host);
 int rts_solve_read_ibar(rts_ctx* ctx, double* ibar_host);
 
 /* ---------------------------------------------------------------------- */
+/* batched problems: one persistent tensor-core launch per step            */
+/* ---------------------------------------------------------------------- */
+/* Many independent scattering problems (own cell count, direction set,
+ * phase kernel, precision, frequency groups, albedo) are kept resident and
+ * advanced together: every step is one launch of the grouped tcgen05 kernel
+ * over the tiles of all problems (source update, residual and relaxation
+ * fused), and a fixed number of steps can be captured into a CUDA graph and
+ * replayed.  No counterpart in the reference, which solves one problem per
+ * process. */
+typedef struct rts_batch rts_batch;
+
+typedef struct rts_problem_desc {
+    int64_t N;      /* cells per frequency group */
+    int64_t M;      /* directions: spherical Fibonacci set of M points, weights 4 pi / M */
+    int64_t groups; /* frequency groups sharing the direction set and phase kernel (>= 1) */
+    int phase;      /* RTS_PHASE_THOMSON or RTS_PHASE_HG */
+    double g;       /* Henyey-Greenstein asymmetry, (-1, 1) */
+    int precision;  /* RTS_PREC_FP16X3 or RTS_PREC_BF16X3 */
+    int flush;      /* hi*hi drain period in blocks of 32 in-directions (0: 1) */
+    int bn;         /* out-directions per tile, multiple of 16, <= 128 (0: balanced default) */
+} rts_problem_desc;
+
+/* Device bytes a problem holds while resident (for admission control). */
+int rts_problem_footprint(const rts_problem_desc* desc, int64_t* bytes);
+
+int rts_batch_create(rts_ctx* ctx, rts_batch** out);
+int rts_batch_destroy(rts_batch* batch);
+
+/* Adds a problem.  ibar: host [groups][M][N] FP32 face-mean intensity
+ * (direction-major, as grid_t::scattering); B: host [groups][N] FP32 source;
+ * lambda: host [groups] albedo.  The copies complete before the call returns. */
+int rts_batch_add(rts_batch* batch, const rts_problem_desc* desc, const float* ibar, const float* B,
+                  const double* lambda, int64_t* id);
+int rts_batch_remove(rts_batch* batch, int64_t id);
+int rts_batch_size(rts_batch* batch, int64_t* problems, int64_t* tiles);
+
+/* One step of every problem (relax != 0: Ibar <- 0.5 Ibar + 0.5 S after it). */
+int rts_batch_step(rts_batch* batch, int relax);
+
+/* Captures `steps` steps into a CUDA graph (invalidated by add / remove) and
+ * replays it. */
+int rts_batch_capture(rts_batch* batch, int steps, int relax);
+int rts_batch_replay(rts_batch* batch);
+
+/* Waits for the batch's work with a deadline (timeout_us < 0: no limit). */
+int rts_batch_sync(rts_batch* batch, int64_t timeout_us);
+
+/* S [groups][M][N] FP32 of a problem (host), and the FP64 residual
+ * max|S - S_prev| of its last step (either may be NULL); synchronous. */
+int rts_batch_read(rts_batch* batch, int64_t id, float* S, double* residual);
+
+/* ---------------------------------------------------------------------- */
+/* serving: continuous batching of scattering solves                       */
+/* ---------------------------------------------------------------------- */
+typedef struct rts_request {
+    double arrival_s;       /* arrival, seconds after the start of the run (non-decreasing) */
+    rts_problem_desc desc;  /* the problem */
+    int iterations;         /* source iterations to run (relaxation after each) */
+    const float* ibar;      /* host [groups][M][N] FP32 initial face-mean intensity */
+    const float* B;         /* host [groups][N] FP32 source */
+    const double* lambda;   /* host [groups] albedo */
+    float* S_out;           /* host [groups][M][N] result, or NULL */
+} rts_request;
+
+typedef struct rts_serve_stats {
+    int64_t completed, rejected, max_active, steps, peak_bytes;
+    double makespan_s;
+    double throughput;      /* cell-direction-iterations per second */
+    double p50_ms, p99_ms, mean_ms, max_ms;
+} rts_serve_stats;
+
+/* Runs the requests through one device batch with continuous batching:
+ * arrived requests are admitted in arrival order while the context's device
+ * bytes stay under hbm_cap, every step advances all resident requests by one
+ * iteration in one grouped launch, finished requests are read back and leave.
+ * latency_ms[i] (may be NULL) receives request i's latency, -1 if rejected.
+ * step_timeout_us bounds every device wait.  No counterpart in the reference. */
+int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, int64_t hbm_cap, int64_t step_timeout_us,
+                  double* latency_ms, rts_serve_stats* stats);
+
+/* Pinned host memory (for request inputs and results). */
+int rts_host_alloc(int64_t bytes, void** ptr);
+int rts_host_free(void* ptr);
+
+/* ---------------------------------------------------------------------- */
 /* synthetic inputs (benchmark workloads; not part of the reference API)   */
 /* ---------------------------------------------------------------------- */
 

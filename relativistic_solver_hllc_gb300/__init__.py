@@ -16,6 +16,7 @@ from ._native import (  # noqa: F401
     STREAM_PARAMS,
     STREAM_SCATTERING_1,
     STREAM_SCATTERING_2,
+    Batch,
     Context,
     RtsError,
     header_symbols,

@@ -178,6 +178,27 @@ def synth_uniform(seed: int, stream: int, lo: float, hi: float, n: int, i0: int 
         raise RtsError(rc, "rts_synth_uniform")
     return out
 
+class ProblemDesc(C.Structure):
+    """rts_problem_desc"""
+    _fields_ = [("N", C.c_int64), ("M", C.c_int64), ("groups", C.c_int64), ("phase", C.c_int), ("g", C.c_double),
+                ("precision", C.c_int), ("flush", C.c_int), ("bn", C.c_int)]
+
+
+_SIGNATURES.update({
+    "rts_problem_footprint": (C.c_int, [C.POINTER(ProblemDesc), C.POINTER(_i64)]),
+    "rts_batch_create": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "rts_batch_destroy": (C.c_int, [_vp]),
+    "rts_batch_add": (C.c_int, [_vp, C.POINTER(ProblemDesc), C.POINTER(C.c_float), C.POINTER(C.c_float), _dp,
+                                C.POINTER(_i64)]),
+    "rts_batch_remove": (C.c_int, [_vp, _i64]),
+    "rts_batch_size": (C.c_int, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
+    "rts_batch_step": (C.c_int, [_vp, C.c_int]),
+    "rts_batch_capture": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "rts_batch_replay": (C.c_int, [_vp]),
+    "rts_batch_sync": (C.c_int, [_vp, _i64]),
+    "rts_batch_read": (C.c_int, [_vp, _i64, C.POINTER(C.c_float), _dp]),
+})
+
 _lib = None
 
 
@@ -467,3 +488,140 @@ class Context:
             self.lib.rts_synth_illum(self.h, C.c_uint64(seed), float(mu), float(sigma), int(bool(independent_faces))),
             "rts_synth_illum",
         )
+
+
+def problem_desc(N, M, groups=1, phase=PHASE_THOMSON, g=0.0, precision="fp16x3", flush=0, bn=0) -> ProblemDesc:
+    prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    return ProblemDesc(int(N), int(M), int(groups), int(phase), float(g), prec, int(flush), int(bn))
+
+
+def problem_footprint(desc: ProblemDesc) -> int:
+    v = _i64()
+    _status(load_library().rts_problem_footprint(C.byref(desc), C.byref(v)), "rts_problem_footprint")
+    return v.value
+
+
+class Batch:
+    """Resident scattering problems advanced together (one grouped launch per step)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = _vp()
+        ctx._check(self.lib.rts_batch_create(ctx.h, C.byref(h)), "rts_batch_create")
+        self.h = h
+        self.shapes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rts_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add(self, desc: ProblemDesc, ibar, B, lam) -> int:
+        """ibar [groups][M][N] FP32, B [groups][N] FP32, lam [groups]."""
+        ibar = np.ascontiguousarray(ibar, dtype=np.float32)
+        B = np.ascontiguousarray(B, dtype=np.float32)
+        lam = np.ascontiguousarray(np.atleast_1d(lam), dtype=np.float64)
+        G, M, N = desc.groups, desc.M, desc.N
+        if ibar.size != G * M * N or B.size != G * N or lam.size != G:
+            raise ValueError("input sizes do not match the descriptor")
+        pid = _i64()
+        fp = C.POINTER(C.c_float)
+        self.ctx._check(self.lib.rts_batch_add(self.h, C.byref(desc), ibar.ctypes.data_as(fp), B.ctypes.data_as(fp),
+                                               _ptr(lam), C.byref(pid)), "rts_batch_add")
+        self.shapes[pid.value] = (G, M, N)
+        return pid.value
+
+    def remove(self, pid: int):
+        self.ctx._check(self.lib.rts_batch_remove(self.h, int(pid)), "rts_batch_remove")
+        self.shapes.pop(pid, None)
+
+    def size(self):
+        p, t = _i64(), _i64()
+        self.ctx._check(self.lib.rts_batch_size(self.h, C.byref(p), C.byref(t)), "rts_batch_size")
+        return p.value, t.value
+
+    def step(self, relax: bool = False):
+        self.ctx._check(self.lib.rts_batch_step(self.h, int(bool(relax))), "rts_batch_step")
+
+    def capture(self, steps: int, relax: bool = False):
+        self.ctx._check(self.lib.rts_batch_capture(self.h, int(steps), int(bool(relax))), "rts_batch_capture")
+
+    def replay(self):
+        self.ctx._check(self.lib.rts_batch_replay(self.h), "rts_batch_replay")
+
+    def sync(self, timeout_us: int = -1):
+        self.ctx._check(self.lib.rts_batch_sync(self.h, int(timeout_us)), "rts_batch_sync")
+
+    def read(self, pid: int):
+        G, M, N = self.shapes[pid]
+        S = np.empty(G * M * N, dtype=np.float32)
+        r = C.c_double()
+        self.ctx._check(self.lib.rts_batch_read(self.h, int(pid), S.ctypes.data_as(C.POINTER(C.c_float)), C.byref(r)),
+                        "rts_batch_read")
+        return S.reshape(G, M, N), r.value
+
+
+class Request(C.Structure):
+    """rts_request"""
+    _fields_ = [("arrival_s", C.c_double), ("desc", ProblemDesc), ("iterations", C.c_int),
+                ("ibar", C.POINTER(C.c_float)), ("B", C.POINTER(C.c_float)), ("lambda_", _dp),
+                ("S_out", C.POINTER(C.c_float))]
+
+
+class ServeStats(C.Structure):
+    """rts_serve_stats"""
+    _fields_ = [("completed", C.c_int64), ("rejected", C.c_int64), ("max_active", C.c_int64), ("steps", C.c_int64),
+                ("peak_bytes", C.c_int64), ("makespan_s", C.c_double), ("throughput", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double)]
+
+
+_SIGNATURES.update({
+    "rts_serve_run": (C.c_int, [_vp, C.POINTER(Request), _i64, _i64, _i64, _dp, C.POINTER(ServeStats)]),
+    "rts_host_alloc": (C.c_int, [_i64, C.POINTER(_vp)]),
+    "rts_host_free": (C.c_int, [_vp]),
+})
+
+
+def serve(ctx: Context, requests, hbm_cap: int, step_timeout_us: int = 10_000_000):
+    """Run a list of Request structures (sorted by arrival) through the
+    continuous-batching loop; returns (stats, latencies_ms)."""
+    n = len(requests)
+    arr = (Request * n)(*requests)
+    lat = np.empty(max(n, 1))
+    st = ServeStats()
+    ctx._check(ctx.lib.rts_serve_run(ctx.h, arr, n, int(hbm_cap), int(step_timeout_us), _ptr(lat), C.byref(st)),
+               "rts_serve_run")
+    return st, lat[:n]
+
+
+class PinnedBuffer:
+    """Pinned host memory from the library (rts_host_alloc)."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load_library()
+        p = _vp()
+        _status(self.lib.rts_host_alloc(int(nbytes), C.byref(p)), "rts_host_alloc")
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def array(self, dtype, count, offset_bytes: int = 0):
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dtype, count=count, offset=offset_bytes)
+
+    def close(self):
+        if self.ptr:
+            self.lib.rts_host_free(C.c_void_p(self.ptr))
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,186 @@
+// rts_batch.cu -- public C ABI of batched problems (include/rts_scatter.h,
+// "batched problems"): admission of problems with their inputs, one grouped
+// launch per step, CUDA-graph capture / replay, read-back.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "rts_group.h"
+#include "rts_internal.h"
+
+namespace {
+
+int check_desc(rts_ctx* ctx, const rts_problem_desc* d)
+{
+    RTS_REQUIRE(ctx, d, RTS_ERR_INVALID_ARGUMENT, "null problem descriptor");
+    RTS_REQUIRE(ctx, d->N > 0 && d->M > 0 && d->groups > 0, RTS_ERR_INVALID_ARGUMENT,
+                "problem sizes must be positive (N=%lld M=%lld groups=%lld)", (long long)d->N, (long long)d->M,
+                (long long)d->groups);
+    RTS_REQUIRE(ctx, d->M <= 65536 && d->N * d->groups <= ((int64_t)1 << 36), RTS_ERR_INVALID_ARGUMENT,
+                "problem too large (M=%lld, rows=%lld)", (long long)d->M, (long long)(d->N * d->groups));
+    RTS_REQUIRE(ctx, d->phase == RTS_PHASE_THOMSON || d->phase == RTS_PHASE_HG, RTS_ERR_INVALID_ARGUMENT,
+                "phase must be RTS_PHASE_THOMSON or RTS_PHASE_HG");
+    RTS_REQUIRE(ctx, d->phase != RTS_PHASE_HG || (d->g > -1.0 && d->g < 1.0), RTS_ERR_INVALID_ARGUMENT,
+                "HG asymmetry %g outside (-1, 1)", d->g);
+    RTS_REQUIRE(ctx, d->precision == RTS_PREC_FP16X3 || d->precision == RTS_PREC_BF16X3, RTS_ERR_INVALID_ARGUMENT,
+                "batched problems run the tensor-core precisions only");
+    RTS_REQUIRE(ctx, d->flush >= 0 && d->flush <= 1024, RTS_ERR_INVALID_ARGUMENT, "flush %d outside [0,1024]", d->flush);
+    RTS_REQUIRE(ctx, d->bn == 0 || (d->bn % 16 == 0 && d->bn >= 16 && d->bn <= 128), RTS_ERR_INVALID_ARGUMENT,
+                "bn %d must be a multiple of 16 in [16,128]", d->bn);
+    return RTS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rts_problem_footprint(const rts_problem_desc* desc, int64_t* bytes)
+{
+    if (!desc || !bytes || desc->N <= 0 || desc->M <= 0 || desc->groups <= 0) return RTS_ERR_INVALID_ARGUMENT;
+    *bytes = rts_group_footprint(desc->N, desc->M, desc->groups, true);
+    return RTS_OK;
+}
+
+int rts_batch_create(rts_ctx* ctx, rts_batch** out)
+{
+    if (!ctx || !out) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return rts_group_batch_new(ctx, out);
+}
+
+int rts_batch_destroy(rts_batch* batch)
+{
+    rts_group_batch_free(batch);
+    return RTS_OK;
+}
+
+int rts_batch_add(rts_batch* batch, const rts_problem_desc* d, const float* ibar, const float* B, const double* lambda,
+                  int64_t* id)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    rts_ctx* ctx = rts_group_ctx(batch);
+    int rc = check_desc(ctx, d);
+    if (rc != RTS_OK) return rc;
+    RTS_REQUIRE(ctx, ibar && B && lambda, RTS_ERR_INVALID_ARGUMENT, "rts_batch_add: null input");
+    const int64_t N = d->N, M = d->M, G = d->groups, rows = N * G;
+    for (int64_t g = 0; g < G; ++g)
+        RTS_REQUIRE(ctx, lambda[g] >= 0.0 && lambda[g] <= 1.0, RTS_ERR_INVALID_ARGUMENT,
+                    "albedo %g of group %lld outside [0, 1]", lambda[g], (long long)g);
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+
+    // direction set and W in scratch, followed by the FP32 Ibar staging area
+    std::vector<double> xyz(3 * (size_t)M), area((size_t)M);
+    double full_area = 0.0;
+    rts_synth_directions(M, xyz.data(), area.data(), &full_area);
+    double *d_xyz = nullptr, *d_area = nullptr;
+    rc = rts_group_dirs(batch, xyz.data(), area.data(), M, &d_xyz, &d_area);
+    if (rc != RTS_OK) return rc;
+    const size_t w_bytes = (size_t)(M * M) * 8, i_bytes = (size_t)(rows * M) * 4;
+    void* scratch = nullptr;
+    rc = rts_group_scratch(batch, w_bytes + i_bytes, &scratch);
+    if (rc != RTS_OK) return rc;
+    double* W = static_cast<double*>(scratch);
+    float* stage = reinterpret_cast<float*>(static_cast<char*>(scratch) + w_bytes);
+    rc = rts_launch_weights_raw(ctx, d_xyz, d_area, (int)M, 0, (int)M, full_area, d->phase, d->g, W, st);
+    if (rc != RTS_OK) return rc;
+
+    GProb* p = nullptr;
+    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, d->precision == RTS_PREC_FP16X3, d->flush, d->bn, true, &p);
+    if (rc != RTS_OK) return rc;
+    std::vector<float> lam((size_t)G);
+    for (int64_t g = 0; g < G; ++g) lam[(size_t)g] = (float)lambda[g];
+    cudaError_t e = cudaMemcpyAsync(stage, ibar, i_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->B, B, (size_t)rows * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p->lam, lam.data(), (size_t)G * 4, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        int64_t tmp = 0;
+        rts_group_attach(batch, p, &tmp);  // owned by the batch from here; remove frees it
+        rts_group_remove(batch, tmp);
+        return rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: copy failed: %s", cudaGetErrorString(e));
+    }
+    rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->fp16, p->rs, p->rows_pad, p->a[0], st);
+    if (rc == RTS_OK) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: %s", cudaGetErrorString(e));
+    }
+    int64_t new_id = 0;
+    rts_group_attach(batch, p, &new_id);
+    if (rc != RTS_OK) {
+        rts_group_remove(batch, new_id);
+        return rc;
+    }
+    if (id) *id = new_id;
+    return RTS_OK;
+}
+
+int rts_batch_remove(rts_batch* batch, int64_t id)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    return rts_group_remove(batch, id);
+}
+
+int rts_batch_size(rts_batch* batch, int64_t* problems, int64_t* tiles)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    if (problems) *problems = (int64_t)rts_group_count(batch);
+    if (tiles) *tiles = rts_group_total_tiles(batch);
+    return RTS_OK;
+}
+
+int rts_batch_step(rts_batch* batch, int relax)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    rts_ctx* ctx = rts_group_ctx(batch);
+    return rts_group_step(batch, relax ? 1 : 0, ctx->streams[RTS_STREAM_SCATTERING_1]);
+}
+
+int rts_batch_capture(rts_batch* batch, int steps, int relax)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    return rts_group_capture(batch, steps, relax ? 1 : 0);
+}
+
+int rts_batch_replay(rts_batch* batch)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    return rts_group_replay(batch);
+}
+
+int rts_batch_sync(rts_batch* batch, int64_t timeout_us)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    rts_ctx* ctx = rts_group_ctx(batch);
+    int rc = rts_sync_stream(ctx, RTS_STREAM_SCATTERING_1, timeout_us);
+    if (rc != RTS_OK) return rc;
+    int flag = 0;
+    RTS_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return rts_fail(ctx, RTS_ERR_DEVICE_WAIT, "batched kernel reported device flag %d", flag);
+    return RTS_OK;
+}
+
+int rts_batch_read(rts_batch* batch, int64_t id, float* S, double* residual)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    rts_ctx* ctx = rts_group_ctx(batch);
+    GProb* p = rts_group_find(batch, id, nullptr);
+    RTS_REQUIRE(ctx, p, RTS_ERR_INVALID_ARGUMENT, "no problem with id %lld in the batch", (long long)id);
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    if (S)
+        RTS_CUDA_TRY(ctx, cudaMemcpyAsync(S, p->S32, (size_t)(p->rows * p->Mout) * 4, cudaMemcpyDeviceToHost, st));
+    unsigned long long bits = 0;
+    if (residual) {
+        if (p->slot >= 0)
+            RTS_CUDA_TRY(ctx, cudaMemcpyAsync(&bits, rts_group_resid_slot(batch, (size_t)p->slot), sizeof(bits),
+                                              cudaMemcpyDeviceToHost, st));
+    }
+    RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if (residual) memcpy(residual, &bits, sizeof(double));
+    int flag = 0;
+    RTS_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return rts_fail(ctx, RTS_ERR_DEVICE_WAIT, "batched kernel reported device flag %d", flag);
+    return RTS_OK;
+}
+
+}  // extern "C"

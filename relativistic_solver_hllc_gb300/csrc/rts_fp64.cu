@@ -466,3 +466,13 @@ extern "C" int rts_scattering_noalloc(const double* d_illum, const double* d_xyz
     if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
     return RTS_OK;
 }
+
+// W [M][loc] of an arbitrary direction set on `st` (used by the batched path).
+int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_area, int M, int k_off, int loc,
+                           double full_area, int phase, double g, double* W, cudaStream_t st)
+{
+    weights_kernel<<<(loc + 127) / 128, 128, 0, st>>>(d_xyz, d_area, M, k_off, loc, full_area, phase, g, W);
+    RTS_CHECK_LAUNCH(ctx, "weights_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}

@@ -1,0 +1,478 @@
+// rts_group.cu -- batched split-precision scattering integrals: many
+// independent problems (own cell count, direction set, phase kernel,
+// precision, groups, albedo) resident on the device, one persistent grouped
+// tcgen05 launch per source-iteration step, optionally replayed from a CUDA
+// graph.  The context's own source iteration (rts_solve_*) and host-buffer
+// calls (rts_scattering_update) run on the same kernel through private
+// one-problem batches (rts_split.cu).
+//
+// Reference counterpart: the reference solves one problem per process and
+// launches d_GetS_MPI_Stream per call (cuda/cuda_solve.cu:89-111); batching,
+// graphs and admission have no counterpart there.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rts_group.h"
+#include "rts_internal.h"
+#include "rts_ptx.cuh"
+
+namespace {
+#include "rts_group_kernel.cuh"
+
+int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn(rts_ctx* ctx)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (fn) return fn;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p) {
+        cudaGetLastError();
+        rts_fail(ctx, RTS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        return nullptr;
+    }
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return fn;
+}
+
+// 2-D map over interleaved split rows [rows][2*kpad] (16-bit): box of 64
+// halves x box_rows, 128-byte swizzle.
+int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t kpad, int box_rows)
+{
+    auto enc = encode_fn(ctx);
+    if (!enc) return RTS_ERR_CUDA;
+    cuuint64_t dims[2] = {(cuuint64_t)(2 * kpad), (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(2 * kpad * 2)};
+    cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1u, 1u};
+    CUresult r = enc(reinterpret_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base),
+                     dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return rts_fail(ctx, RTS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for %lld x %lld", (int)r,
+                        (long long)rows, (long long)(2 * kpad));
+    return RTS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// problem and batch objects
+// ---------------------------------------------------------------------------
+struct rts_batch {
+    rts_ctx* ctx = nullptr;
+    std::vector<GProb*> probs;
+    int64_t next_id = 1;
+    GroupProblem* d_table = nullptr;
+    size_t table_cap = 0;
+    std::vector<GroupProblem> h_table;
+    bool dirty = true;
+    int table_relax = -1;
+    unsigned long long* d_resid = nullptr;
+    size_t resid_cap = 0;
+    void* staging = nullptr;  // FP32 Ibar / FP64 W scratch for set-up
+    size_t staging_bytes = 0;
+    double* d_dirs = nullptr;  // xyz + area scratch
+    size_t dirs_cap = 0;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_steps = 0, graph_relax = 0;
+    int64_t total_tiles = 0;
+    int64_t steps = 0;
+};
+
+namespace {
+
+void free_prob(rts_ctx* ctx, GProb* p)
+{
+    const size_t abytes = (size_t)(p->rows_pad * 2 * p->kpad * 2);
+    rts_dfree(ctx, p->wc, (size_t)(p->mpad * 2 * p->kpad * 2));
+    rts_dfree(ctx, p->cs, (size_t)(2 * p->mpad * 4));
+    rts_dfree(ctx, p->a[0], abytes);
+    rts_dfree(ctx, p->a[1], abytes);
+    rts_dfree(ctx, p->rs, (size_t)(2 * p->rows_pad * 4));
+    rts_dfree(ctx, p->B, (size_t)(p->rows * 4));
+    rts_dfree(ctx, p->lam, (size_t)(p->groups * 4));
+    rts_dfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4));
+    delete p;
+}
+
+void drop_graph(rts_batch* b)
+{
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    b->graph_steps = 0;
+}
+
+int ensure_scratch(rts_batch* b, size_t bytes)
+{
+    if (b->staging_bytes >= bytes) return RTS_OK;
+    cudaStreamSynchronize(b->ctx->streams[RTS_STREAM_SCATTERING_1]);
+    rts_dfree(b->ctx, b->staging, b->staging_bytes);
+    b->staging = nullptr;
+    b->staging_bytes = 0;
+    int rc = rts_dmalloc(b->ctx, &b->staging, bytes, "batch staging");
+    if (rc == RTS_OK) b->staging_bytes = bytes;
+    return rc;
+}
+
+}  // namespace
+
+// Tile geometry of a problem: out-direction tiles of at most 128, balanced.
+void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override, int* bn, int* n_tiles,
+                        int64_t* kpad, int64_t* mpad, int64_t* rows_pad, int64_t* m_tiles)
+{
+    int b = bn_override;
+    if (b <= 0) {
+        const int64_t nt = (Mout + G_BN - 1) / G_BN;
+        b = (int)round_up((Mout + nt - 1) / nt, 16);
+    }
+    b = std::min(std::max(b, 16), G_BN);
+    *bn = b;
+    *n_tiles = (int)((Mout + b - 1) / b);
+    *mpad = (int64_t)(*n_tiles) * b;
+    *kpad = round_up(Min, 32);
+    *rows_pad = round_up(rows, G_BM);
+    *m_tiles = *rows_pad / G_BM;
+}
+
+int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative)
+{
+    int bn, nt;
+    int64_t kpad, mpad, rows_pad, mt;
+    const int64_t rows = N * groups;
+    rts_group_geometry(M, M, rows, 0, &bn, &nt, &kpad, &mpad, &rows_pad, &mt);
+    int64_t bytes = mpad * 2 * kpad * 2 + 2 * mpad * 4 + 2 * rows_pad * 4 + rows * 4 + groups * 4;
+    bytes += (iterative ? 2 : 1) * rows_pad * 2 * kpad * 2;
+    if (iterative) bytes += rows * M * 4;
+    return bytes;
+}
+
+// Creates a problem: allocations, W (phase kernel on the given directions)
+// split into rows, tensor maps.  A rows, B and lambda are filled by the caller.
+int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev,
+                          int ldw, bool fp16, int flush, int bn_override, bool iterative, GProb** out)
+{
+    rts_ctx* ctx = b->ctx;
+    GProb* p = new GProb();
+    p->N = N;
+    p->M = Min;
+    p->Mout = Mout;
+    p->groups = groups;
+    p->rows = N * groups;
+    p->fp16 = fp16;
+    p->flush = flush > 0 ? flush : 1;
+    rts_group_geometry(Min, Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad, &p->rows_pad,
+                       &p->m_tiles);
+    int rc;
+    void* q;
+#define GP_ALLOC(field, nbytes, name)                                 \
+    if ((rc = rts_dmalloc(ctx, &q, (nbytes), name)) != RTS_OK) {      \
+        free_prob(ctx, p);                                            \
+        return rc;                                                    \
+    }                                                                 \
+    p->field = (decltype(p->field))q;                                 \
+    p->bytes += (nbytes);
+    const size_t abytes = (size_t)(p->rows_pad * 2 * p->kpad * 2);
+    GP_ALLOC(wc, (size_t)(p->mpad * 2 * p->kpad * 2), "split W");
+    GP_ALLOC(cs, (size_t)(2 * p->mpad * 4), "W column scales");
+    GP_ALLOC(a[0], abytes, "split Ibar");
+    if (iterative) {
+        GP_ALLOC(a[1], abytes, "split Ibar (next)");
+    }
+    GP_ALLOC(rs, (size_t)(2 * p->rows_pad * 4), "Ibar row scales");
+    GP_ALLOC(B, (size_t)(p->rows * 4), "source B");
+    GP_ALLOC(lam, (size_t)(p->groups * 4), "albedo");
+    if (iterative) {
+        GP_ALLOC(S32, (size_t)(p->rows * p->Mout * 4), "FP32 scattering");
+    }
+#undef GP_ALLOC
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
+    if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
+    if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
+    rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, fp16, p->wc, p->cs, st);
+    if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->kpad, p->bn);
+    if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->kpad, G_BM);
+    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->kpad, G_BM);
+    if (rc != RTS_OK) {
+        free_prob(ctx, p);
+        return rc;
+    }
+    if (!p->a[1]) memcpy(p->maps[1], p->maps[0], 128);
+    *out = p;
+    return RTS_OK;
+}
+
+int rts_group_attach(rts_batch* b, GProb* p, int64_t* id)
+{
+    p->id = b->next_id++;
+    b->probs.push_back(p);
+    b->dirty = true;
+    drop_graph(b);
+    if (id) *id = p->id;
+    return RTS_OK;
+}
+
+GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index)
+{
+    for (size_t i = 0; i < b->probs.size(); ++i)
+        if (b->probs[i]->id == id) {
+            if (index) *index = i;
+            return b->probs[i];
+        }
+    return nullptr;
+}
+
+int rts_group_batch_new(rts_ctx* ctx, rts_batch** out)
+{
+    rts_batch* b = new rts_batch();
+    b->ctx = ctx;
+    *out = b;
+    return RTS_OK;
+}
+
+void rts_group_batch_free(rts_batch* b)
+{
+    if (!b) return;
+    rts_ctx* ctx = b->ctx;
+    cudaStreamSynchronize(ctx->streams[RTS_STREAM_SCATTERING_1]);
+    drop_graph(b);
+    for (GProb* p : b->probs) free_prob(ctx, p);
+    rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));
+    rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
+    rts_dfree(ctx, b->staging, b->staging_bytes);
+    rts_dfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double));
+    delete b;
+}
+
+// Build the device table for the next launch(es).
+static int upload_table(rts_batch* b, int relax, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    if (!b->dirty && b->table_relax == relax) return RTS_OK;
+    const size_t n = b->probs.size();
+    if (n > b->table_cap) {
+        cudaStreamSynchronize(st);
+        rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));
+        rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
+        b->d_table = nullptr;
+        b->d_resid = nullptr;
+        b->table_cap = b->resid_cap = 0;
+        const size_t cap = std::max<size_t>(16, n * 2);
+        void* q;
+        int rc = rts_dmalloc(ctx, &q, cap * sizeof(GroupProblem), "batch table");
+        if (rc != RTS_OK) return rc;
+        b->d_table = (GroupProblem*)q;
+        rc = rts_dmalloc(ctx, &q, cap * sizeof(unsigned long long), "batch residuals");
+        if (rc != RTS_OK) return rc;
+        b->d_resid = (unsigned long long*)q;
+        b->table_cap = b->resid_cap = cap;
+    }
+    b->h_table.assign(n, GroupProblem());
+    int64_t tiles = 0;
+    for (size_t i = 0; i < n; ++i) {
+        GProb* p = b->probs[i];
+        GroupProblem& g = b->h_table[i];
+        memset(&g, 0, sizeof(g));
+        memcpy(&g.mapA[0], p->maps[0], 128);
+        memcpy(&g.mapA[1], p->maps[1], 128);
+        memcpy(&g.mapW, p->maps[2], 128);
+        g.N = p->N;
+        g.rows = p->rows;
+        g.tile_begin = tiles;
+        g.m_tiles = (int)p->m_tiles;
+        g.n_tiles = p->n_tiles;
+        g.Mout = (int)p->Mout;
+        g.kpad = (int)p->kpad;
+        g.kblocks = (int)(p->kpad / 32);
+        g.bn = p->bn;
+        g.flush = p->flush;
+        g.groups = (int)p->groups;
+        g.idesc = rts_ptx::idesc_f16(p->fp16, G_BM, p->bn);
+        g.fp16 = p->fp16 ? 1 : 0;
+        g.cur = p->cur;
+        const bool iterative = p->S32 != nullptr;
+        g.relax = (iterative && relax && p->a[1] && p->Mout == p->M) ? 1 : 0;
+        g.residual = iterative ? 1 : 0;
+        g.rs = p->fp16 ? p->rs : nullptr;
+        g.rs_inv = p->fp16 ? p->rs + p->rows_pad : nullptr;
+        g.cs_inv = p->fp16 ? p->cs + p->mpad : nullptr;
+        g.B = p->use_B ? p->B : nullptr;
+        g.lam = p->lam;
+        g.S32 = p->S32;
+        g.S64 = p->S64;
+        g.a[0] = p->a[0];
+        g.a[1] = p->a[1] ? p->a[1] : p->a[0];
+        g.resid = b->d_resid + i;
+        p->slot = (int)i;
+        tiles += p->m_tiles * p->n_tiles;
+    }
+    b->total_tiles = tiles;
+    if (n) RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_table.data(), n * sizeof(GroupProblem),
+                                             cudaMemcpyHostToDevice, st));
+    // the pageable source must outlive the copy
+    RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    b->dirty = false;
+    b->table_relax = relax;
+    return RTS_OK;
+}
+
+static int enqueue_step(rts_batch* b, int relax, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    const int n = (int)b->probs.size();
+    RTS_CUDA_TRY(ctx, cudaMemsetAsync(b->d_resid, 0, n * sizeof(unsigned long long), st));
+    const int64_t grid = std::min<int64_t>(ctx->num_sms, b->total_tiles);
+    if (grid > 0) {
+        rts_timing_begin(ctx, st);
+        group_kernel<<<(unsigned)grid, G_THREADS, G_SMEM, st>>>(b->d_table, n, b->total_tiles, ctx->d_flag);
+        rts_timing_end(ctx, st);
+        RTS_CHECK_LAUNCH(ctx, "group_kernel");
+        ctx->launches++;
+    }
+    if (relax) {
+        group_flip_kernel<<<(n + 127) / 128, 128, 0, st>>>(b->d_table, n);
+        RTS_CHECK_LAUNCH(ctx, "group_flip_kernel");
+        ctx->launches++;
+    }
+    return RTS_OK;
+}
+
+static void host_flip(rts_batch* b, int relax, int times)
+{
+    if (!relax || !(times & 1)) return;
+    for (size_t i = 0; i < b->probs.size(); ++i) {
+        GProb* p = b->probs[i];
+        if (p->S32 && p->a[1]) {
+            p->cur ^= 1;
+            b->h_table[i].cur ^= 1;  // the device table was flipped in place
+        }
+    }
+}
+
+int rts_group_step(rts_batch* b, int relax, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED,
+                "the tensor-core path needs a Blackwell (sm_10x) device, found sm_%d%d", ctx->cc_major, ctx->cc_minor);
+    if (b->probs.empty()) return RTS_OK;
+    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    int rc = upload_table(b, relax, st);
+    if (rc != RTS_OK) return rc;
+    rc = enqueue_step(b, relax, st);
+    if (rc != RTS_OK) return rc;
+    host_flip(b, relax, 1);
+    b->steps++;
+    return RTS_OK;
+}
+
+int rts_group_capture(rts_batch* b, int steps, int relax)
+{
+    rts_ctx* ctx = b->ctx;
+    RTS_REQUIRE(ctx, steps > 0 && steps <= 4096, RTS_ERR_INVALID_ARGUMENT, "graph steps %d outside [1,4096]", steps);
+    RTS_REQUIRE(ctx, !b->probs.empty(), RTS_ERR_BAD_STATE, "capture of an empty batch");
+    RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell device");
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    int rc = upload_table(b, relax, st);
+    if (rc != RTS_OK) return rc;
+    drop_graph(b);
+    const bool was_timing = ctx->timing;
+    ctx->timing = false;  // no event records inside the graph
+    RTS_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int64_t launches0 = ctx->launches;
+    for (int s = 0; s < steps && rc == RTS_OK; ++s) rc = enqueue_step(b, relax, st);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    ctx->timing = was_timing;
+    ctx->launches = launches0;  // counted when the graph is replayed
+    if (rc != RTS_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return rts_fail(ctx, RTS_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        b->gexec = nullptr;
+        return rts_fail(ctx, RTS_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    b->graph_steps = steps;
+    b->graph_relax = relax;
+    return RTS_OK;
+}
+
+int rts_group_replay(rts_batch* b)
+{
+    rts_ctx* ctx = b->ctx;
+    RTS_REQUIRE(ctx, b->gexec && !b->dirty, RTS_ERR_BAD_STATE,
+                "no captured graph (or the batch changed since the capture)");
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    rts_timing_begin(ctx, st);
+    RTS_CUDA_TRY(ctx, cudaGraphLaunch(b->gexec, st));
+    rts_timing_end(ctx, st);
+    ctx->launches += (int64_t)b->graph_steps * (b->graph_relax ? 2 : 1);
+    host_flip(b, b->graph_relax, b->graph_steps);
+    b->steps += b->graph_steps;
+    return RTS_OK;
+}
+
+int64_t rts_group_total_tiles(rts_batch* b) { return b->total_tiles; }
+rts_ctx* rts_group_ctx(rts_batch* b) { return b->ctx; }
+size_t rts_group_count(rts_batch* b) { return b->probs.size(); }
+unsigned long long* rts_group_resid_slot(rts_batch* b, size_t index) { return b->d_resid + index; }
+int rts_group_scratch(rts_batch* b, size_t bytes, void** p)
+{
+    int rc = ensure_scratch(b, bytes);
+    if (rc == RTS_OK) *p = b->staging;
+    return rc;
+}
+
+int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t M, double** d_xyz, double** d_area)
+{
+    rts_ctx* ctx = b->ctx;
+    const size_t need = (size_t)(4 * M);
+    if (b->dirs_cap < need) {
+        cudaStreamSynchronize(ctx->streams[RTS_STREAM_SCATTERING_1]);
+        rts_dfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double));
+        b->d_dirs = nullptr;
+        b->dirs_cap = 0;
+        void* q;
+        int rc = rts_dmalloc(ctx, &q, need * sizeof(double), "batch directions");
+        if (rc != RTS_OK) return rc;
+        b->d_dirs = (double*)q;
+        b->dirs_cap = need;
+    }
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_dirs, xyz, (size_t)(3 * M) * 8, cudaMemcpyHostToDevice, st));
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_dirs + 3 * M, area, (size_t)M * 8, cudaMemcpyHostToDevice, st));
+    *d_xyz = b->d_dirs;
+    *d_area = b->d_dirs + 3 * M;
+    return RTS_OK;
+}
+
+int rts_group_remove(rts_batch* b, int64_t id)
+{
+    size_t idx = 0;
+    GProb* p = rts_group_find(b, id, &idx);
+    RTS_REQUIRE(b->ctx, p, RTS_ERR_INVALID_ARGUMENT, "no problem with id %lld in the batch", (long long)id);
+    cudaStreamSynchronize(b->ctx->streams[RTS_STREAM_SCATTERING_1]);
+    free_prob(b->ctx, p);
+    b->probs.erase(b->probs.begin() + (long)idx);
+    b->dirty = true;
+    drop_graph(b);
+    return RTS_OK;
+}
+
+void rts_group_invalidate(rts_batch* b)
+{
+    if (!b) return;
+    b->dirty = true;
+    drop_graph(b);
+}

@@ -1,0 +1,59 @@
+// rts_group.h -- internal interface of the batched tensor-core path
+// (rts_group.cu): resident problems and one-launch-per-step batches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+
+#include "rts_scatter.h"
+
+struct rts_ctx;
+struct rts_batch;
+
+// One resident problem: split operands, scales, source, albedo, output.
+struct GProb {
+    int64_t id = 0;
+    int64_t N = 0, M = 0, Mout = 0, groups = 1, rows = 0, rows_pad = 0, kpad = 0, mpad = 0;  // M: in-directions
+    int bn = 0, n_tiles = 0, flush = 1;
+    int64_t m_tiles = 0;
+    bool fp16 = true;
+    uint16_t* wc = nullptr;  // [mpad][2*kpad] split W^T rows
+    float* cs = nullptr;     // [2*mpad]: column scale, inverse
+    uint16_t* a[2] = {nullptr, nullptr};  // [rows_pad][2*kpad] split Ibar rows (ping-pong)
+    float* rs = nullptr;     // [2*rows_pad]: row scale, inverse
+    float* B = nullptr;      // [rows]
+    float* lam = nullptr;    // [groups]
+    float* S32 = nullptr;    // [groups][Mout][N] (source iteration)
+    double* S64 = nullptr;   // [groups][Mout][N] FP64 output (host-buffer calls), not owned
+    bool use_B = true;       // false: the bare integral (no source update)
+    int cur = 0;
+    int slot = -1;           // index of the problem's residual in the last launched table
+    size_t bytes = 0;
+    alignas(64) unsigned char maps[3][128];
+};
+
+void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override, int* bn, int* n_tiles, int64_t* kpad,
+                        int64_t* mpad, int64_t* rows_pad, int64_t* m_tiles);
+int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative);
+int rts_group_batch_new(rts_ctx* ctx, rts_batch** out);
+void rts_group_batch_free(rts_batch* b);
+int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev, int ldw,
+                          bool fp16, int flush, int bn_override, bool iterative, GProb** out);
+int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
+GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
+int rts_group_remove(rts_batch* b, int64_t id);
+int rts_group_step(rts_batch* b, int relax, cudaStream_t st);
+int rts_group_capture(rts_batch* b, int steps, int relax);
+int rts_group_replay(rts_batch* b);
+int64_t rts_group_total_tiles(rts_batch* b);
+size_t rts_group_count(rts_batch* b);
+unsigned long long* rts_group_resid_slot(rts_batch* b, size_t index);
+int rts_group_scratch(rts_batch* b, size_t bytes, void** p);
+int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t M, double** d_xyz,
+                   double** d_area);
+rts_ctx* rts_group_ctx(rts_batch* b);
+// Forces the device table to be rebuilt before the next launch (after the
+// caller changed cur / S64 / use_B of a problem) and drops a captured graph.
+void rts_group_invalidate(rts_batch* b);

@@ -40,22 +40,14 @@ int rts_fail(rts_ctx* ctx, int status, const char* fmt, ...);
 constexpr int64_t RTS_RESID_CAP = 4096;
 
 // Split-precision operands of one source iteration (tensor-core path).
+struct rts_batch;
 struct rts_split_state {
-    int precision = -1;
-    int64_t kpad = 0;       // in-direction count padded to the K block
-    int64_t mpad = 0;       // out-direction count padded to the N tile
-    int64_t npad = 0;       // cell count padded to the M tile
-    void* w_hi = nullptr;   // [mpad][kpad] 16-bit, K-major
-    void* w_lo = nullptr;
-    void* i_hi[2] = {nullptr, nullptr};  // [npad][kpad] 16-bit, K-major, ping-pong
-    void* i_lo[2] = {nullptr, nullptr};
-    float* w_colscale = nullptr;   // per out-direction scale folded into W (FP16 mode)
-    float* i_rowscale[2] = {nullptr, nullptr};  // per cell scale of Ibar (FP16 mode)
-    float* s32 = nullptr;   // [M][N] FP32 scattering of the tensor path
-    int cur = 0;            // which ping-pong buffer holds the current Ibar
-    int bn = 0;             // out-directions per tile
-    // TMA descriptors (CUtensorMap, 128 bytes each): A buffer 0, A buffer 1, W
-    alignas(64) unsigned char maps[3][128] = {};
+    int precision = -1;             // precision of the resident source iteration
+    rts_batch* iter = nullptr;      // one-problem batch of the source iteration
+    int64_t iter_id = 0;
+    int shot_precision = -1;        // precision of the host-buffer problem
+    rts_batch* shot = nullptr;      // one-problem batch of host-buffer calls (FP64 S out)
+    int64_t shot_id = 0;
 };
 
 struct rts_ctx {
@@ -129,6 +121,21 @@ int rts_launch_update(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t
 int rts_launch_relax_fp64(rts_ctx* ctx, cudaStream_t st);
 int rts_launch_weights(rts_ctx* ctx);
 int rts_launch_synth(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int independent_faces);
+
+int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_area, int M, int k_off, int loc,
+                           double full_area, int phase, double g, double* W, cudaStream_t st);
+
+// Operand preparation of the split-precision path (rts_prepass.cu).
+int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, bool fp16,
+                   uint16_t* Wc, float* cs, cudaStream_t st);
+int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int M, int kpad, const double* B, bool fp16,
+                           float* rs, int64_t npad, uint16_t* A, cudaStream_t st);
+int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
+                         bool fp16, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st);
+int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
+                     bool fp16, double* out, cudaStream_t st);
+int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
+int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 
 // Tensor-core path (rts_split.cu).
 int rts_split_setup(rts_ctx* ctx, int precision);

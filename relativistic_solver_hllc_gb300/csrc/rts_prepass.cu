@@ -1,0 +1,282 @@
+// rts_prepass.cu -- operand preparation of the split-precision path.
+//
+// Every tensor-core contraction reads its operands as "interleaved split"
+// rows of 16-bit values: for each group of 32 in-directions, 32 high parts
+// followed by 32 low parts (128 bytes), x*scale = hi + lo.  These kernels
+// build them:
+//   * W^T rows (one per out-direction) from the FP64 direction-pair matrix,
+//     with a power-of-two column scale in FP16 mode;
+//   * Ibar rows (one per cell) from the reference's face-layout Illum
+//     [M][N][4] FP64 (face mean in the reference's order, then split), or from
+//     a direction-major FP32 Ibar [groups][M][N];
+//   * per-row power-of-two scales (FP16 mode) putting max(|Ibar|, |B|) * 2
+//     into [2^13, 2^14), so hi + lo keeps 22 bits with 4x headroom to 65504;
+//   * the inverse (rows back to FP64 Ibar) for inspection.
+// All are HBM-bound: the Illum prepass reads 32 B and writes 4 B per
+// (cell, direction).  Transposes go through shared memory so both the
+// direction-major reads and the cell-major writes are coalesced.
+#include <cstdint>
+
+#include "rts_internal.h"
+#include "rts_ptx.cuh"
+
+using namespace rts_ptx;
+
+namespace {
+
+__device__ __forceinline__ float pow2_scale(double m)
+{
+    if (!(m > 0.0) || !isfinite(m)) return 1.0f;
+    return ldexpf(1.0f, 13 - ilogb(m));
+}
+
+// W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
+__global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad, int mpad,
+                               int fp16, uint16_t* __restrict__ Wc, float* __restrict__ cs)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= mpad) return;
+    uint16_t* row = Wc + (int64_t)k * 2 * kpad;
+    float* cs_inv = cs + mpad;
+    if (k >= Mout) {
+        for (int j = 0; j < 2 * kpad; ++j) row[j] = 0;
+        cs[k] = 1.0f;
+        cs_inv[k] = 1.0f;
+        return;
+    }
+    float s = 1.0f;
+    if (fp16) {
+        double m = 0.0;
+        for (int j = 0; j < Min; ++j) m = fmax(m, fabs(W[(int64_t)j * ldw + k]));
+        s = pow2_scale(m);
+    }
+    for (int j = 0; j < kpad; ++j) {
+        uint16_t hi = 0, lo = 0;
+        if (j < Min) split_any(fp16 != 0, (float)(W[(int64_t)j * ldw + k] * (double)s), hi, lo);
+        row[ilv_hi(j)] = hi;
+        row[ilv_hi(j) + 32] = lo;
+    }
+    cs[k] = s;
+    cs_inv[k] = 1.0f / s;
+}
+
+__device__ __forceinline__ double face_mean(const double* __restrict__ illum, int64_t N, int j, int64_t c)
+{
+    const double2* p = reinterpret_cast<const double2*>(illum + ((int64_t)j * N + c) * 4);
+    const double2 a = __ldg(p), b = __ldg(p + 1);
+    double I = 0.0;  // faces 0..3 in order, then /4 (GET_FACE_TO_CELL)
+    I += a.x;
+    I += a.y;
+    I += b.x;
+    I += b.y;
+    return I / 4;
+}
+
+// Row scales from the face layout: thread per cell.
+__global__ void rowscale_faces_kernel(const double* __restrict__ illum, int64_t N, int M,
+                                      const double* __restrict__ B, float* __restrict__ rs, int64_t npad)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= npad) return;
+    float s = 1.0f;
+    if (c < N) {
+        double m = B ? fabs(B[c]) : 0.0;
+        for (int j = 0; j < M; ++j) m = fmax(m, fabs(face_mean(illum, N, j, c)));
+        s = pow2_scale(2.0 * m);
+    }
+    rs[c] = s;
+    rs[npad + c] = 1.0f / s;
+}
+
+// Row scales from direction-major FP32 Ibar [groups][M][N]: thread per row.
+__global__ void rowscale_f32_kernel(const float* __restrict__ ibar, int64_t N, int M, int64_t rows,
+                                    const float* __restrict__ B, float* __restrict__ rs, int64_t rows_pad)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows_pad) return;
+    float s = 1.0f;
+    if (r < rows) {
+        const int64_t g = r / N, c = r - g * N;
+        const float* base = ibar + g * (int64_t)M * N + c;
+        double m = B ? fabs((double)B[r]) : 0.0;
+        for (int j = 0; j < M; ++j) m = fmax(m, fabs((double)base[(int64_t)j * N]));
+        s = pow2_scale(2.0 * m);
+    }
+    rs[r] = s;
+    rs[rows_pad + r] = 1.0f / s;
+}
+
+// Transpose-and-split through shared memory.  Tile: 32 in-directions x 64
+// rows, 256 threads.  `Src` supplies the value of (direction j, row r).
+template <class Src>
+__device__ __forceinline__ void split_tile(const Src& src, int64_t rows, int M, int kpad, const float* __restrict__ rs,
+                                           int fp16, uint16_t* __restrict__ A)
+{
+    __shared__ float tile[64][33];
+    const int j0 = blockIdx.y * 32;
+    const int64_t r0 = (int64_t)blockIdx.x * 64;
+    const int t = threadIdx.x;
+    {
+        const int rr = t & 63;
+        const int64_t r = r0 + rr;
+        const float s = (r < rows && rs) ? rs[r] : 1.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int jj = (t >> 6) + 4 * q;
+            const int j = j0 + jj;
+            tile[rr][jj] = (r < rows && j < M) ? (float)(src(j, r) * (double)s) : 0.0f;
+        }
+    }
+    __syncthreads();
+    const int rr = t >> 2;
+    const int part = t & 3;  // 0,1: hi of j 0-15 / 16-31; 2,3: lo of j 0-15 / 16-31
+    const int64_t r = r0 + rr;
+    if (r >= rows) return;
+    const int jbase = (part & 1) * 16;
+    uint16_t out[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        uint16_t hi, lo;
+        split_any(fp16 != 0, tile[rr][jbase + i], hi, lo);
+        out[i] = (part < 2) ? hi : lo;
+    }
+    uint16_t* dst = A + r * 2 * (int64_t)kpad + (int64_t)(j0 >> 5) * 64 + (part >= 2 ? 32 : 0) + jbase;
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    d4[0] = make_uint4(pack2(out[0], out[1]), pack2(out[2], out[3]), pack2(out[4], out[5]), pack2(out[6], out[7]));
+    d4[1] = make_uint4(pack2(out[8], out[9]), pack2(out[10], out[11]), pack2(out[12], out[13]),
+                       pack2(out[14], out[15]));
+}
+
+struct FacesSrc {
+    const double* illum;
+    int64_t N;
+    __device__ double operator()(int j, int64_t c) const { return face_mean(illum, N, j, c); }
+};
+
+struct F32Src {
+    const float* ibar;
+    int64_t N;
+    int M;
+    __device__ double operator()(int j, int64_t r) const
+    {
+        const int64_t g = r / N, c = r - g * N;
+        return (double)__ldg(ibar + (g * M + j) * N + c);
+    }
+};
+
+__global__ void __launch_bounds__(256) split_faces_kernel(const double* __restrict__ illum, int64_t N, int M, int kpad,
+                                                          const float* __restrict__ rs, int fp16,
+                                                          uint16_t* __restrict__ A)
+{
+    split_tile(FacesSrc{illum, N}, N, M, kpad, rs, fp16, A);
+}
+
+__global__ void __launch_bounds__(256) split_f32_kernel(const float* __restrict__ ibar, int64_t N, int M,
+                                                        int64_t rows, int kpad, const float* __restrict__ rs,
+                                                        int fp16, uint16_t* __restrict__ A)
+{
+    split_tile(F32Src{ibar, N, M}, rows, M, kpad, rs, fp16, A);
+}
+
+// Rows back to direction-major FP64 Ibar [groups][M][N].
+__global__ void join_rows_kernel(const uint16_t* __restrict__ A, int64_t N, int M, int64_t rows, int kpad,
+                                 const float* __restrict__ rs_inv, int fp16, double* __restrict__ out)
+{
+    const int64_t total = (int64_t)M * rows;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        // i enumerates [g][j][c]
+        const int64_t g = i / ((int64_t)M * N);
+        const int64_t rem = i - g * (int64_t)M * N;
+        const int64_t j = rem / N, c = rem - j * N;
+        const int64_t r = g * N + c;
+        const uint16_t* row = A + r * 2 * (int64_t)kpad;
+        const float x = join_any(fp16 != 0, row[ilv_hi(j)], row[ilv_hi(j) + 32]);
+        out[i] = (double)x * (double)(rs_inv ? rs_inv[r] : 1.0f);
+    }
+}
+
+__global__ void f32_to_f64_kernel(const float* __restrict__ s, double* __restrict__ d, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = (double)s[i];
+}
+
+__global__ void f64_to_f32_kernel(const double* __restrict__ s, float* __restrict__ d, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = (float)s[i];
+}
+
+int blocks_for(rts_ctx* ctx, int64_t n, int threads)
+{
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)ctx->num_sms * 16;
+    return (int)(b > cap ? cap : (b < 1 ? 1 : b));
+}
+
+}  // namespace
+
+int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, bool fp16,
+                   uint16_t* Wc, float* cs, cudaStream_t st)
+{
+    split_w_kernel<<<(mpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, mpad, fp16 ? 1 : 0, Wc, cs);
+    RTS_CHECK_LAUNCH(ctx, "split_w_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int M, int kpad, const double* B, bool fp16,
+                           float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
+{
+    if (fp16) {
+        rowscale_faces_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(illum, N, M, B, rs, npad);
+        RTS_CHECK_LAUNCH(ctx, "rowscale_faces_kernel");
+        ctx->launches++;
+    }
+    dim3 grid((unsigned)((N + 63) / 64), (unsigned)(kpad / 32));
+    split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, M, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
+    RTS_CHECK_LAUNCH(ctx, "split_faces_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
+                         bool fp16, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st)
+{
+    if (fp16) {
+        rowscale_f32_kernel<<<(unsigned)((rows_pad + 127) / 128), 128, 0, st>>>(ibar, N, M, rows, B, rs, rows_pad);
+        RTS_CHECK_LAUNCH(ctx, "rowscale_f32_kernel");
+        ctx->launches++;
+    }
+    dim3 grid((unsigned)((rows + 63) / 64), (unsigned)(kpad / 32));
+    split_f32_kernel<<<grid, 256, 0, st>>>(ibar, N, M, rows, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
+    RTS_CHECK_LAUNCH(ctx, "split_f32_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
+                     bool fp16, double* out, cudaStream_t st)
+{
+    join_rows_kernel<<<blocks_for(ctx, (int64_t)M * rows, 256), 256, 0, st>>>(A, N, M, rows, kpad, rs_inv,
+                                                                              fp16 ? 1 : 0, out);
+    RTS_CHECK_LAUNCH(ctx, "join_rows_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st)
+{
+    f32_to_f64_kernel<<<blocks_for(ctx, n, 256), 256, 0, st>>>(s, d, n);
+    RTS_CHECK_LAUNCH(ctx, "f32_to_f64_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st)
+{
+    f64_to_f32_kernel<<<blocks_for(ctx, n, 256), 256, 0, st>>>(s, d, n);
+    RTS_CHECK_LAUNCH(ctx, "f64_to_f32_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}

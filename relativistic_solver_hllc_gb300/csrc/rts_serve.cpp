@@ -1,0 +1,191 @@
+// rts_serve.cpp -- continuous-batching request loop for scattering solves.
+//
+// Requests (a problem with its inputs and a number of source iterations)
+// arrive over time.  One host thread drives one device batch:
+//   * admission: arrived requests join the batch in arrival order as long as
+//     the context's device bytes plus the request's resident footprint stay
+//     under the HBM cap; a request larger than the cap is rejected;
+//   * every step advances every resident request by one source iteration in
+//     one grouped tcgen05 launch, so requests that arrive while others run
+//     share the device from their first step on;
+//   * a request that has run its iterations is read back (S, FP32) and
+//     leaves the batch, freeing its memory for waiting requests.
+// Latency = completion time - arrival time (host wall clock).  Waits on the
+// device are bounded; nothing here blocks forever.
+//
+// No counterpart in the reference (one solve per process).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <thread>
+#include <vector>
+
+#include "rts_group.h"
+#include "rts_internal.h"
+
+namespace {
+
+using clock_type = std::chrono::steady_clock;
+
+double seconds_since(clock_type::time_point t0)
+{
+    return std::chrono::duration<double>(clock_type::now() - t0).count();
+}
+
+double percentile(std::vector<double> v, double q)
+{
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double pos = q * (double)(v.size() - 1);
+    const size_t lo = (size_t)std::floor(pos), hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
+}
+
+struct Active {
+    int64_t req = 0;
+    int64_t id = 0;
+    int remaining = 0;
+    int64_t bytes = 0;
+};
+
+}  // namespace
+
+extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, int64_t hbm_cap, int64_t step_timeout_us,
+                             double* latency_ms, rts_serve_stats* stats)
+{
+    if (!ctx || (n > 0 && !reqs) || n < 0 || !stats) return RTS_ERR_INVALID_ARGUMENT;
+    for (int64_t i = 0; i < n; ++i) {
+        RTS_REQUIRE(ctx, reqs[i].iterations > 0, RTS_ERR_INVALID_ARGUMENT, "request %lld has no iterations",
+                    (long long)i);
+        RTS_REQUIRE(ctx, i == 0 || reqs[i].arrival_s >= reqs[i - 1].arrival_s, RTS_ERR_INVALID_ARGUMENT,
+                    "requests must be sorted by arrival time");
+    }
+    memset(stats, 0, sizeof(*stats));
+    for (int64_t i = 0; i < n; ++i)
+        if (latency_ms) latency_ms[i] = -1.0;
+    rts_batch* batch = nullptr;
+    int rc = rts_batch_create(ctx, &batch);
+    if (rc != RTS_OK) return rc;
+
+    std::deque<int64_t> waiting;
+    std::vector<Active> active;
+    std::vector<double> lat;
+    int64_t next = 0, done = 0, rejected = 0, steps = 0, peak = ctx->used_bytes, max_active = 0;
+    double work = 0.0;  // cell-direction-iterations completed
+    const int64_t base_bytes = ctx->used_bytes;
+    const auto t0 = clock_type::now();
+
+    while (done + rejected < n) {
+        const double now = seconds_since(t0);
+        while (next < n && reqs[next].arrival_s <= now) waiting.push_back(next++);
+        // admission in arrival order while the HBM cap allows
+        while (!waiting.empty()) {
+            const int64_t r = waiting.front();
+            int64_t fp = 0;
+            rts_problem_footprint(&reqs[r].desc, &fp);
+            const rts_problem_desc& d = reqs[r].desc;
+            // transient set-up scratch: FP64 W and FP32 Ibar staging
+            const int64_t scratch = d.M * d.M * 8 + d.N * d.groups * d.M * 4;
+            if (base_bytes + fp + scratch > hbm_cap) {  // can never fit
+                waiting.pop_front();
+                ++rejected;
+                continue;
+            }
+            if (ctx->used_bytes + fp + scratch > hbm_cap && !active.empty()) break;
+            int64_t id = 0;
+            rc = rts_batch_add(batch, &d, reqs[r].ibar, reqs[r].B, reqs[r].lambda, &id);
+            if (rc == RTS_ERR_OVER_BUDGET || rc == RTS_ERR_OUT_OF_MEMORY) {
+                if (active.empty()) {  // nothing will free memory: reject
+                    waiting.pop_front();
+                    ++rejected;
+                    continue;
+                }
+                break;
+            }
+            if (rc != RTS_OK) {
+                rts_batch_destroy(batch);
+                return rc;
+            }
+            active.push_back(Active{r, id, reqs[r].iterations, fp});
+            waiting.pop_front();
+            peak = std::max(peak, ctx->used_bytes);
+        }
+        max_active = std::max<int64_t>(max_active, (int64_t)active.size());
+        if (active.empty()) {
+            if (next < n) {
+                const double wait = reqs[next].arrival_s - seconds_since(t0);
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+                continue;
+            }
+            break;  // only rejected requests were left
+        }
+        rc = rts_batch_step(batch, 1);
+        if (rc == RTS_OK) rc = rts_batch_sync(batch, step_timeout_us);
+        if (rc != RTS_OK) {
+            rts_batch_destroy(batch);
+            return rc;
+        }
+        ++steps;
+        // completions
+        for (size_t i = 0; i < active.size();) {
+            Active& a = active[i];
+            if (--a.remaining > 0) {
+                ++i;
+                continue;
+            }
+            const rts_request& q = reqs[a.req];
+            rc = rts_batch_read(batch, a.id, q.S_out, nullptr);
+            if (rc == RTS_OK) rc = rts_batch_remove(batch, a.id);
+            if (rc != RTS_OK) {
+                rts_batch_destroy(batch);
+                return rc;
+            }
+            const double l = (seconds_since(t0) - q.arrival_s) * 1e3;
+            if (latency_ms) latency_ms[a.req] = l;
+            lat.push_back(l);
+            work += (double)q.desc.N * (double)q.desc.groups * (double)q.desc.M * (double)q.iterations;
+            ++done;
+            active[i] = active.back();
+            active.pop_back();
+        }
+    }
+    const double makespan = seconds_since(t0);
+    rts_batch_destroy(batch);
+    stats->completed = done;
+    stats->rejected = rejected;
+    stats->max_active = max_active;
+    stats->steps = steps;
+    stats->makespan_s = makespan;
+    stats->throughput = makespan > 0 ? work / makespan : 0.0;
+    stats->p50_ms = percentile(lat, 0.50);
+    stats->p99_ms = percentile(lat, 0.99);
+    double sum = 0, mx = 0;
+    for (double v : lat) {
+        sum += v;
+        mx = std::max(mx, v);
+    }
+    stats->mean_ms = lat.empty() ? 0.0 : sum / (double)lat.size();
+    stats->max_ms = mx;
+    stats->peak_bytes = peak;
+    return RTS_OK;
+}
+
+extern "C" int rts_host_alloc(int64_t bytes, void** ptr)
+{
+    if (!ptr || bytes <= 0) return RTS_ERR_INVALID_ARGUMENT;
+    *ptr = nullptr;
+    if (cudaMallocHost(ptr, (size_t)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return RTS_ERR_OUT_OF_MEMORY;
+    }
+    return RTS_OK;
+}
+
+extern "C" int rts_host_free(void* ptr)
+{
+    if (ptr) cudaFreeHost(ptr);
+    return RTS_OK;
+}
