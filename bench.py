@@ -61,7 +61,57 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
+                    help="2: the headline source iteration (default); 1, 3, 4, 5: the other configurations")
     return ap.parse_args()
+
+
+def run_other_config(args, rank, world, local):
+    """Configurations 1, 3, 4, 5 (bench_configs.py): one JSON line each."""
+    import torch
+
+    import bench_configs as bc
+    import relativistic_solver_hllc_gb300 as pkg
+    from relativistic_solver_hllc_gb300 import _native
+
+    pkg.build_library()
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    K, W = args.steps, args.warmup
+    prec = args.precision if args.precision != "fp64" else "fp16x3"
+    clocks = ClockSampler(local)
+    clocks.start()
+    if args.config == 1:
+        res = bc.config1(pkg, _native, ctx, torch, K, W)
+        dtype = "f64"
+    elif args.config == 3:
+        res = bc.config3(pkg, _native, ctx, torch, K, W, prec)
+        res["bf16x3"] = bc.config3(pkg, _native, ctx, torch, K, W, "bf16x3") if prec != "bf16x3" else None
+        dtype = prec
+    elif args.config == 4:
+        res = bc.config4(pkg, _native, ctx, torch, K, W, prec)
+        dtype = prec
+    else:
+        res = bc.config5(pkg, _native, ctx, torch, precision=prec)
+        dtype = prec
+    clk = clocks.stop()
+    if args.config == 5:
+        row80 = next((r for r in res["loads"] if abs(r["load"] - 0.8) < 1e-9), res["loads"][-1])
+        line = {"metric": METRIC, "value": row80["throughput_cell_dir_iter_per_s"] / 1e9, "unit": UNIT,
+                "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+                "config": {"workload": "config5: serving stream, Poisson arrivals 10-120% of saturation, "
+                                       "HG, M in {110,302,590,1202}, 5-40 iterations, 120 GB cap"},
+                "serve": res, "p50_ms_at_80pct": row80["p50_ms"], "p99_ms_at_80pct": row80["p99_ms"], "clocks": clk}
+    else:
+        line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": dtype, "data": "synthetic",
+                "config": {"workload": f"config{args.config}: " + res.pop("workload")}, "result": res,
+                "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
 
 
 def dist_env():
@@ -387,6 +437,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)
+    elif args.config != 2:
+        run_other_config(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

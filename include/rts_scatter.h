@@ -344,6 +344,18 @@ int rts_host_free(void* ptr);
  * (j*N+c)*4+f with independent_faces). */
 int rts_synth_illum(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int independent_faces);
 
+/* Adds a batched problem whose inputs are generated on the device from the
+ * counter hash: Ibar [g][j][c] lognormal(mu, sigma) (stream 1, index
+ * (g*M + j)*N + c), B [g][c] uniform(b_lo, b_hi) (stream 2, index g*N + c). */
+int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc* desc, uint64_t seed, double mu, double sigma,
+                            double b_lo, double b_hi, const double* lambda, int64_t* id);
+
+/* n values of the counter hash (stream, indices i0..i0+n) generated on the
+ * device and copied to host memory: lognormal(a, b) if lognormal != 0, else
+ * uniform(a, b). */
+int rts_synth_host_f32(rts_ctx* ctx, uint64_t seed, uint64_t stream, int lognormal, double a, double b, int64_t i0,
+                       int64_t n, float* host_out);
+
 /* Spherical Fibonacci direction set: xyz [M][3], area [M] = 4 pi / M,
  * full_area = 4 pi (host only, no context needed). */
 int rts_synth_directions(int64_t M, double* xyz, double* area, double* full_area);
@@ -381,9 +393,9 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
 /* ---------------------------------------------------------------------- */
 
 /* Tuning knobs of the tensor-core path (0 restores the default):
- *   RTS_TUNE_FLUSH: in-direction blocks of 32 accumulated on the tensor core
- *   before the hi*hi partial sum is added in FP32 on the CUDA cores
- *   (default 1; smaller is more accurate, larger issues fewer drains). */
+ *   RTS_TUNE_FLUSH: in-direction blocks of 32 (1 or 2) accumulated on the
+ *   tensor core before the partial sum is added in FP32 on the CUDA cores
+ *   (default 1; 1 is more accurate, 2 issues half as many drains). */
 #define RTS_TUNE_FLUSH 1
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 

@@ -197,6 +197,10 @@ _SIGNATURES.update({
     "rts_batch_replay": (C.c_int, [_vp]),
     "rts_batch_sync": (C.c_int, [_vp, _i64]),
     "rts_batch_read": (C.c_int, [_vp, _i64, C.POINTER(C.c_float), _dp]),
+    "rts_batch_add_synthetic": (C.c_int, [_vp, C.POINTER(ProblemDesc), C.c_uint64, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, _dp, C.POINTER(_i64)]),
+    "rts_synth_host_f32": (C.c_int, [_vp, C.c_uint64, C.c_uint64, C.c_int, C.c_double, C.c_double, _i64, _i64,
+                                     C.POINTER(C.c_float)]),
 })
 
 _lib = None
@@ -483,6 +487,19 @@ class Context:
                     "rts_kernel_timing")
         return ms.value, n.value
 
+    def synth_host_f32(self, seed: int, stream: int, lognormal: bool, a: float, b: float, n: int, i0: int = 0,
+                       out: np.ndarray | None = None) -> np.ndarray:
+        """n counter-hash values (indices i0..i0+n of `stream`) generated on the
+        device into a host FP32 array: lognormal(a, b) or uniform(a, b)."""
+        if out is None:
+            out = np.empty(int(n), dtype=np.float32)
+        if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < n:
+            raise ValueError("out must be a contiguous float32 array of at least n values")
+        self._check(self.lib.rts_synth_host_f32(self.h, C.c_uint64(seed), C.c_uint64(stream), int(bool(lognormal)),
+                                                float(a), float(b), int(i0), int(n),
+                                                out.ctypes.data_as(C.POINTER(C.c_float))), "rts_synth_host_f32")
+        return out
+
     def synth_illum(self, seed: int, mu: float, sigma: float, independent_faces: bool = False):
         self._check(
             self.lib.rts_synth_illum(self.h, C.c_uint64(seed), float(mu), float(sigma), int(bool(independent_faces))),
@@ -536,6 +553,20 @@ class Batch:
         self.ctx._check(self.lib.rts_batch_add(self.h, C.byref(desc), ibar.ctypes.data_as(fp), B.ctypes.data_as(fp),
                                                _ptr(lam), C.byref(pid)), "rts_batch_add")
         self.shapes[pid.value] = (G, M, N)
+        return pid.value
+
+    def add_synthetic(self, desc: ProblemDesc, seed: int, mu: float, sigma: float, b_lo: float, b_hi: float,
+                      lam) -> int:
+        """A problem whose Ibar (lognormal(mu, sigma)) and B (uniform(b_lo, b_hi))
+        are generated on the device from the counter hash."""
+        lam = np.ascontiguousarray(np.atleast_1d(lam), dtype=np.float64)
+        if lam.size != desc.groups:
+            raise ValueError("lambda needs one value per group")
+        pid = _i64()
+        self.ctx._check(self.lib.rts_batch_add_synthetic(self.h, C.byref(desc), C.c_uint64(seed), float(mu),
+                                                         float(sigma), float(b_lo), float(b_hi), _ptr(lam),
+                                                         C.byref(pid)), "rts_batch_add_synthetic")
+        self.shapes[pid.value] = (desc.groups, desc.M, desc.N)
         return pid.value
 
     def remove(self, pid: int):

@@ -692,8 +692,8 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     switch (key) {
     case RTS_TUNE_FLUSH:
-        RTS_REQUIRE(ctx, value >= 0 && value <= 1024, RTS_ERR_INVALID_ARGUMENT,
-                    "flush period %d outside [0, 1024]", value);
+        RTS_REQUIRE(ctx, value >= 0 && value <= 2, RTS_ERR_INVALID_ARGUMENT,
+                    "flush period %d outside [0, 2]", value);
         ctx->split_flush = value;
         return RTS_OK;
     default:

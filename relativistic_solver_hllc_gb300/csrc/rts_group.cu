@@ -166,7 +166,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     p->groups = groups;
     p->rows = N * groups;
     p->fp16 = fp16;
-    p->flush = flush > 0 ? flush : 1;
+    p->flush = std::min(std::max(flush, 1), G_MAX_FLUSH);
     rts_group_geometry(Min, Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad, &p->rows_pad,
                        &p->m_tiles);
     int rc;
@@ -328,7 +328,7 @@ static int enqueue_step(rts_batch* b, int relax, cudaStream_t st)
     rts_ctx* ctx = b->ctx;
     const int n = (int)b->probs.size();
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(b->d_resid, 0, n * sizeof(unsigned long long), st));
-    const int64_t grid = std::min<int64_t>(ctx->num_sms, b->total_tiles);
+    const int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * G_CTAS_PER_SM, b->total_tiles);
     if (grid > 0) {
         rts_timing_begin(ctx, st);
         group_kernel<<<(unsigned)grid, G_THREADS, G_SMEM, st>>>(b->d_table, n, b->total_tiles, ctx->d_flag);
@@ -423,7 +423,12 @@ int rts_group_replay(rts_batch* b)
     return RTS_OK;
 }
 
-int64_t rts_group_total_tiles(rts_batch* b) { return b->total_tiles; }
+int64_t rts_group_total_tiles(rts_batch* b)
+{
+    int64_t tiles = 0;
+    for (GProb* p : b->probs) tiles += p->m_tiles * p->n_tiles;
+    return tiles;
+}
 rts_ctx* rts_group_ctx(rts_batch* b) { return b->ctx; }
 size_t rts_group_count(rts_batch* b) { return b->probs.size(); }
 unsigned long long* rts_group_resid_slot(rts_batch* b, size_t index) { return b->d_resid + index; }
