@@ -270,7 +270,7 @@ typedef struct rts_problem_desc {
     double g;       /* Henyey-Greenstein asymmetry, (-1, 1) */
     int precision;  /* RTS_PREC_FP16X3 or RTS_PREC_BF16X3 */
     int flush;      /* hi*hi drain period in blocks of 32 in-directions (0: 1) */
-    int bn;         /* out-directions per tile, multiple of 16, <= 128 (0: balanced default) */
+    int bn;         /* out-directions per tile, multiple of 16, <= 256 (0: balanced default) */
 } rts_problem_desc;
 
 /* Device bytes a problem holds while resident (for admission control). */

@@ -28,8 +28,8 @@ int check_desc(rts_ctx* ctx, const rts_problem_desc* d)
     RTS_REQUIRE(ctx, d->precision == RTS_PREC_FP16X3 || d->precision == RTS_PREC_BF16X3, RTS_ERR_INVALID_ARGUMENT,
                 "batched problems run the tensor-core precisions only");
     RTS_REQUIRE(ctx, d->flush >= 0 && d->flush <= 2, RTS_ERR_INVALID_ARGUMENT, "flush %d outside [0,2]", d->flush);
-    RTS_REQUIRE(ctx, d->bn == 0 || (d->bn % 16 == 0 && d->bn >= 16 && d->bn <= 128), RTS_ERR_INVALID_ARGUMENT,
-                "bn %d must be a multiple of 16 in [16,128]", d->bn);
+    RTS_REQUIRE(ctx, d->bn == 0 || (d->bn % 16 == 0 && d->bn >= 16 && d->bn <= 256), RTS_ERR_INVALID_ARGUMENT,
+                "bn %d must be a multiple of 16 in [16,256]", d->bn);
     return RTS_OK;
 }
 

@@ -123,7 +123,7 @@ int ensure_scratch(rts_batch* b, size_t bytes)
 
 }  // namespace
 
-// Tile geometry of a problem: out-direction tiles of at most 128, balanced.
+// Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
 void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override, int* bn, int* n_tiles,
                         int64_t* kpad, int64_t* mpad, int64_t* rows_pad, int64_t* m_tiles)
 {

@@ -2,47 +2,56 @@
 // split-precision scattering integral (included by rts_group.cu).
 //
 // One launch runs one source-iteration step of every problem of a batch: the
-// tiles of all problems (128 cells x up to 128 out-directions each; problems
+// tiles of all problems (128 cells x up to 256 out-directions each; problems
 // of different cell and direction counts, phase kernels and precisions) form
-// one list that persistent CTAs walk with a fixed stride.
+// one list that persistent CTAs (one per SM) walk with a fixed stride.
 //
-// Two CTAs run on every SM.  Measured on GB300, one CTA issuing
-// tcgen05.mma back to back gets one instruction through every ~280 cycles
-// whatever N is, while the SM's tensor core sustains several such streams;
-// two resident CTAs (each with its own issuing thread) double the tensor
-// throughput of the SM, and one CTA's epilogue overlaps the other's main loop.
+// Measured on GB300: a warp that issues tcgen05.mma back to back gets one
+// instruction through every ~300 cycles, whatever N (32..256) or the
+// accumulator is, while the SM's tensor core sustains about four such
+// streams of N = 128 (or two of N = 256).  So a CTA runs two issuing warps,
+// each with N up to 256, on alternate chunks of the in-direction range of the
+// same tile (split K inside the CTA): together they keep the tensor core
+// near its peak while each accumulator is drained in turn.
 //
-// Warp roles (192 threads per CTA):
-//   warp 0      TMA producer: A (split Ibar rows) and B (split W rows)
-//               K-slices into a 3-stage shared-memory ring;
-//   warp 1      TMEM owner (256 columns) and single-thread MMA issuer;
-//   warps 2..5  epilogue: drain the accumulator of every `flush` K-slices into
-//               FP32 registers (round-to-nearest adds; the tensor core
-//               truncates each accumulate), then for the finished tile run the
-//               fused epilogue (unscaling, source update, residual, S store,
-//               relaxation of Ibar in split form).
-// TMEM: two accumulators of 128 columns used alternately per chunk of
-// `flush` K-slices, so the MMAs of one chunk run while the previous chunk is
-// drained.  Within a chunk the cross products hi*lo and lo*hi (2^-11 or 2^-8
-// of the result) are issued first, while the accumulator is still small, and
-// the two hi*hi products last: the truncation then costs about one FP32 ulp of
-// the chunk sum per hi*hi MMA, as with separate accumulators.
+// Warp roles (19 warps, 608 threads, one CTA per SM):
+//   warp 0       TMA producer: A (split Ibar rows) and B (split W rows)
+//                K-slices into a 4-stage shared-memory ring;
+//   warps 1, 2   MMA issuers (one thread each); warp 1 also owns TMEM
+//                (512 columns: one 256-column accumulator per issuer);
+//   warps 3..18  drain + epilogue: warp w reads TMEM lanes 32*(w%4).. and a
+//                64-column slice of the tile.  After every chunk of `flush`
+//                K-slices they add the chunk's accumulator into FP32
+//                registers (round-to-nearest adds: the tensor core truncates
+//                each accumulate) and release it; the tile's sums go back
+//                into its last accumulator, from which the fused epilogue
+//                (unscaling, source update, residual, S store, relaxation of
+//                Ibar in split form) reads them 8 columns at a time while
+//                the other issuer starts the next tile.  Half-way through a
+//                tile these warps prefetch the epilogue's inputs into L2.
+// Within a chunk the cross products hi*lo and lo*hi (2^-11 or 2^-8 of the
+// result) are issued first, while the accumulator is still small, and the two
+// hi*hi products last: the truncation then costs about one FP32 ulp of the
+// chunk sum per hi*hi MMA.
 //
 // Every mbarrier wait is bounded (rts_ptx::mbar_wait); a wait that gives up
 // sets the device flag, every role stops at its next wait, and the kernel
 // drains and exits.
 
 constexpr int G_BM = 128;
-constexpr int G_BN = 128;
-constexpr int G_STAGES = 3;
+constexpr int G_BN = 256;
+constexpr int G_STAGES = 4;
 constexpr int G_A_BYTES = G_BM * 128;
 constexpr int G_B_BYTES = G_BN * 128;
 constexpr int G_STAGE_BYTES = G_A_BYTES + G_B_BYTES;
-constexpr int G_THREADS = 192;
-constexpr int G_CTAS_PER_SM = 2;
-constexpr uint32_t G_TMEM_COLS = 256;
-constexpr int G_MAX_FLUSH = 2;  // chunks are at most 2 K-slices (both resident in the ring)
+constexpr int G_EPI_WARPS = 16;
+constexpr int G_EPI_WARP0 = 3;
+constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
+constexpr int G_CTAS_PER_SM = 1;
+constexpr uint32_t G_TMEM_COLS = 512;
+constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
 constexpr size_t G_SMEM = (size_t)G_STAGES * G_STAGE_BYTES + 1024 + 256;
+static_assert(G_SMEM <= 227 * 1024, "shared memory per CTA");
 
 struct GroupProblem {  // aligned as its CUtensorMap members
     CUtensorMap mapA[2];  // split Ibar, ping-pong buffers
@@ -80,7 +89,7 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
     return lo;
 }
 
-__global__ void __launch_bounds__(G_THREADS, G_CTAS_PER_SM)
+__global__ void __launch_bounds__(G_THREADS, 1)
 group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_tiles, int* flag)
 {
     using namespace rts_ptx;
@@ -103,7 +112,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(acc_full_bar(a), 1);
-            mbar_init(acc_empty_bar(a), 4);
+            mbar_init(acc_empty_bar(a), G_EPI_WARPS);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -145,119 +154,155 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             for (uint32_t i = (it > (uint32_t)G_STAGES ? it - G_STAGES : 0); i < it; ++i)
                 mbar_wait(full_bar(i % G_STAGES), (i / G_STAGES) & 1, flag, FLAG_WAIT_PRODUCER);
         }
-    } else if (warp == 1) {
-        // ------------------------------------------------------------ MMA issuer
+    } else if (warp == 1 || warp == 2) {
+        // ------------------------------------------------------------ MMA issuers
+        const uint32_t me = (uint32_t)(warp - 1);
         if (lane == 0 && live) {
-            uint32_t it = 0, ch = 0;  // K-slice and chunk counters (across tiles)
+            const uint32_t acc = tmem + 256u * me;
+            uint32_t gsl = 0, gch = 0;  // K-slice and chunk counters of this CTA (across tiles)
             bool ok = true;
             for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
                 const GroupProblem& P = probs[find_problem(probs, nprob, t)];
                 const uint32_t idesc = P.idesc;
                 const int nkb = P.kblocks, flush = P.flush;
-                for (int kb0 = 0; kb0 < nkb && ok; kb0 += flush, ++ch) {
+                const int nchunks = (nkb + flush - 1) / flush;
+                for (int c = 0; c < nchunks; ++c) {
+                    const uint32_t g = gch + (uint32_t)c;
+                    if ((g & 1u) != me) continue;
+                    const int kb0 = c * flush;
                     const int f = min(flush, nkb - kb0);
-                    const int a = ch & 1;
-                    const uint32_t acc = tmem + 128u * a;
-                    if (ch >= 2 && !mbar_wait(acc_empty_bar(a), ((ch >> 1) - 1) & 1, flag, FLAG_WAIT_MMA)) {
+                    if (g >= 2 && !mbar_wait(acc_empty_bar(me), ((g >> 1) - 1) & 1, flag, FLAG_WAIT_MMA)) {
                         ok = false;
                         break;
                     }
-                    uint32_t ad[G_MAX_FLUSH], bd[G_MAX_FLUSH];
+                    uint32_t ad[G_MAX_FLUSH], st[G_MAX_FLUSH];
                     for (int j = 0; j < f; ++j) {
-                        const uint32_t i2 = it + j;
-                        const int s = (int)(i2 % G_STAGES);
-                        if (!mbar_wait(full_bar(s), (i2 / G_STAGES) & 1, flag, FLAG_WAIT_MMA)) {
+                        const uint32_t i2 = gsl + (uint32_t)(kb0 + j);
+                        st[j] = i2 % G_STAGES;
+                        if (!mbar_wait(full_bar((int)st[j]), (i2 / G_STAGES) & 1, flag, FLAG_WAIT_MMA)) {
                             ok = false;
                             break;
                         }
-                        ad[j] = smem_base + s * G_STAGE_BYTES;
-                        bd[j] = ad[j] + G_A_BYTES;
+                        ad[j] = smem_base + st[j] * G_STAGE_BYTES;
                     }
                     if (!ok) break;
                     tc_fence_after();
                     const uint64_t hi0 = 0, hi1 = 32 >> 4, lo0 = 64 >> 4, lo1 = 96 >> 4;
                     // cross products first (the accumulator starts from zero), hi*hi last
                     for (int j = 0; j < f; ++j) {
-                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(bd[j]);
+                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
                         umma_f16(acc, A + hi0, Bd + lo0, idesc, j != 0 ? 1u : 0u);
                         umma_f16(acc, A + lo0, Bd + hi0, idesc, 1u);
                         umma_f16(acc, A + hi1, Bd + lo1, idesc, 1u);
                         umma_f16(acc, A + lo1, Bd + hi1, idesc, 1u);
                     }
                     for (int j = 0; j < f; ++j) {
-                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(bd[j]);
+                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
                         umma_f16(acc, A + hi0, Bd + hi0, idesc, 1u);
                         umma_f16(acc, A + hi1, Bd + hi1, idesc, 1u);
                     }
-                    for (int j = 0; j < f; ++j) umma_commit(empty_bar((int)((it + j) % G_STAGES)));
-                    umma_commit(acc_full_bar(a));
-                    it += f;
+                    for (int j = 0; j < f; ++j) umma_commit(empty_bar((int)st[j]));
+                    umma_commit(acc_full_bar((int)me));
                 }
+                gch += (uint32_t)nchunks;
+                gsl += (uint32_t)nkb;
             }
         }
     } else {
-        // ------------------------------------------------------------ epilogue warps
-        const int q = warp & 3;
+        // ------------------------------------------------------------ drain + epilogue warps
+        const int q = warp & 3;                    // TMEM lane quarter
+        const int cs = (warp - G_EPI_WARP0) >> 2;  // 64-column slice of the tile
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        uint32_t ch = 0;
+        uint32_t gch = 0;
         bool ok = live;
         for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
             const GroupProblem& P = probs[find_problem(probs, nprob, t)];
-            // tile parameters, read once into registers
-            const int nkb = P.kblocks, flush = P.flush, bn = P.bn, ng = bn >> 4;
+            const int nkb = P.kblocks, flush = P.flush, bn = P.bn;
             const int nchunks = (nkb + flush - 1) / flush;
+            const int ncols = min(64, bn - 64 * cs);  // columns of this warp (multiple of 16; <= 0: none)
             const int64_t lt = t - P.tile_begin;
             const int m_tile = (int)(lt / P.n_tiles), n_tile = (int)(lt % P.n_tiles);
-            float run[128];
+            float run[64];
 #pragma unroll
-            for (int j = 0; j < 128; ++j) run[j] = 0.0f;
-            uint32_t acc = 0;
-            for (int c = 0; c < nchunks; ++c, ++ch) {
-                const int a = ch & 1;
-                acc = tmem + 128u * a + lane_off;
+            for (int j = 0; j < 64; ++j) run[j] = 0.0f;
+            uint32_t last_acc = 0;
+            int last_a = 0;
+            for (int c = 0; c < nchunks; ++c) {
+                const uint32_t g = gch + (uint32_t)c;
+                const int a = (int)(g & 1u);
+                const uint32_t acc = tmem + 256u * (uint32_t)a + lane_off + 64u * (uint32_t)cs;
                 bool got = true;
-                if (lane == 0) got = mbar_wait(acc_full_bar(a), (ch >> 1) & 1, flag, FLAG_WAIT_EPILOGUE);
+                if (lane == 0) got = mbar_wait(acc_full_bar(a), (g >> 1) & 1, flag, FLAG_WAIT_EPILOGUE);
                 if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                // 32 columns per load-and-wait
 #pragma unroll
-                for (int g = 0; g < 8; g += 2) {
-                    if (g + 1 < ng) {
-                        float v[32];
-                        tmem_ld32(acc + 16u * g, v);
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) run[16 * g + j] += v[j];
-                    } else if (g < ng) {
+                for (int gi = 0; gi < 4; ++gi) {
+                    if (16 * gi < ncols) {
                         float v[16];
-                        tmem_ld16(acc + 16u * g, v);
+                        tmem_ld16(acc + 16u * gi, v);
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) run[16 * g + j] += v[j];
+                        for (int j = 0; j < 16; ++j) run[16 * gi + j] += v[j];
                     }
                 }
                 if (c + 1 < nchunks) {
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(acc_empty_bar(a));
+                    // half-way through the tile, pull the epilogue's inputs (the
+                    // previous S and the Ibar rows it relaxes) into L2
+                    if (c == (nchunks >> 1) && ncols > 0) {
+                        const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
+                        if (r < P.rows) {
+                            const int64_t Nc = P.N;
+                            const int Mout = P.Mout, kb0 = n_tile * bn + 64 * cs;
+                            const int64_t grp = r / Nc;
+                            if (P.S32 && P.residual) {
+                                const float* Sp = P.S32 + grp * (int64_t)Mout * Nc + (r - grp * Nc);
+                                for (int j = 0; j < ncols && kb0 + j < Mout; ++j)
+                                    prefetch_l2(Sp + (int64_t)(kb0 + j) * Nc);
+                            }
+                            if (P.relax && P.S32 && !P.S64 && kb0 < P.kpad) {
+                                const uint16_t* ar = P.a[P.cur] + r * 2 * (int64_t)P.kpad;
+                                const int b0 = kb0 >> 5, b1 = min(kb0 + ncols - 1, P.kpad - 1) >> 5;
+                                for (int b = b0; b <= b1; ++b) prefetch_l2(ar + 64 * (int64_t)b);
+                            }
+                        }
+                    }
+                } else {
+                    // the finished sums go back into the last accumulator, which
+                    // this warp keeps until the epilogue below has read them
+#pragma unroll
+                    for (int gi = 0; gi < 4; ++gi) {
+                        if (16 * gi < ncols) {
+                            float v[16];
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) v[j] = run[16 * gi + j];
+                            tmem_st16(acc + 16u * gi, v);
+                        }
+                    }
+                    tmem_wait_st();
+                    last_acc = acc;
+                    last_a = a;
                 }
             }
+            gch += (uint32_t)nchunks;
             if (!ok) break;
-            // the finished sums go back into the last accumulator, which this
-            // warp keeps until the epilogue below has read them
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                if (g < ng) {
-                    float v[16];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = run[16 * g + j];
-                    tmem_st16(acc + 16u * g, v);
-                }
+            auto release_last = [&]() {
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(acc_empty_bar(last_a));
+            };
+            if (ncols <= 0) {
+                release_last();
+                continue;
             }
-            tmem_wait_st();
 
-            // ---- fused epilogue
+            // ---- fused epilogue, reading the sums back 8 columns at a time:
+            //   S = (1 - lam) B + lam * rs_inv[row] * cs_inv[k] * acc
+            //   Ibar' = 0.5 Ibar + 0.5 rs[row] * S   (relaxation, split again)
             const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
             const int64_t Nc = P.N;
             const int Mout = P.Mout, kpad = P.kpad;
@@ -267,107 +312,105 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const bool fp16 = P.fp16 != 0;
             const bool relax = P.relax != 0, residual = P.residual != 0;
             const float* __restrict__ cs_inv = P.cs_inv;
-            const float rinv = (fp16 && in_row) ? P.rs_inv[r] : 1.0f;
-            const float rsc = (fp16 && in_row) ? P.rs[r] : 1.0f;
             const bool has_B = P.B != nullptr;
             const float lam = (in_row && has_B) ? P.lam[grp] : 1.0f;
+            const float lr = lam * ((fp16 && in_row) ? P.rs_inv[r] : 1.0f);
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
+            const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * Nc + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * Nc + cc : nullptr;
             const int cur = P.cur;
             const uint16_t* __restrict__ arow = P.a[cur] + r * 2 * (int64_t)kpad;
             uint16_t* __restrict__ nrow = P.a[cur ^ 1] + r * 2 * (int64_t)kpad;
-            unsigned long long* resid = P.resid;
-            const int kbase = n_tile * bn;
+            const int kbase = n_tile * bn + 64 * cs;
             float rmax = 0.0f;
             bool overflow = false;
-
-            // global loads of group g+1 are issued before group g is processed
-            float old_n[16];
-            uint4 rh_n[2], rl_n[2];
-#define RTS_EPI_LOAD(G)                                                                                         \
-    do {                                                                                                        \
-        const int k0_ = kbase + 16 * (G);                                                                       \
-        const bool live_ = in_row && k0_ < Mout;                                                                \
-        _Pragma("unroll") for (int j = 0; j < 16; ++j) {                                                        \
-            const bool kj = live_ && k0_ + j < Mout;                                                            \
-            old_n[j] = (kj && residual && S) ? S[(int64_t)(k0_ + j) * Nc] : 0.0f;                              \
-        }                                                                                                       \
-        if (live_ && relax && k0_ < kpad) {                                                                     \
-            const uint4* src_ = reinterpret_cast<const uint4*>(arow + rts_ptx::ilv_hi(k0_));                    \
-            rh_n[0] = src_[0];                                                                                  \
-            rh_n[1] = src_[1];                                                                                  \
-            rl_n[0] = src_[4];                                                                                  \
-            rl_n[1] = src_[5];                                                                                  \
-        } else {                                                                                                \
-            rh_n[0] = rh_n[1] = rl_n[0] = rl_n[1] = make_uint4(0, 0, 0, 0);                                     \
-        }                                                                                                       \
-    } while (0)
-            RTS_EPI_LOAD(0);
 #pragma unroll 1
-            for (int g = 0; g < ng; ++g) {
-                float old[16];
-                uint4 rh[2], rl[2];
+            for (int e0 = 0; e0 < ncols; e0 += 8) {
+                const int k0 = kbase + e0;
+                const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
+                const bool live_k = in_row && nk > 0;
+                const bool do_relax = live_k && relax && !S64;  // relax implies Mout == M <= kpad
+                // global loads first, then the TMEM read
+                float old[8];
+                if (live_k && residual && S) {
+                    const float* sp = S + (int64_t)k0 * Nc;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) old[j] = old_n[j];
-                rh[0] = rh_n[0];
-                rh[1] = rh_n[1];
-                rl[0] = rl_n[0];
-                rl[1] = rl_n[1];
-                if (g + 1 < ng) RTS_EPI_LOAD(g + 1);
-                float v[16];
+                    for (int j = 0; j < 8; ++j, sp += Nc) old[j] = j < nk ? *sp : 0.0f;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) old[j] = 0.0f;
+                }
+                uint4 rh = make_uint4(0, 0, 0, 0), rl = make_uint4(0, 0, 0, 0);
+                if (do_relax) {
+                    const uint4* src = reinterpret_cast<const uint4*>(arow + rts_ptx::ilv_hi(k0));
+                    rh = src[0];
+                    rl = src[4];
+                }
+                float cin[8];
+                if (fp16) {
+                    const float4 c0 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0));
+                    const float4 c1 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0) + 1);
+                    cin[0] = c0.x, cin[1] = c0.y, cin[2] = c0.z, cin[3] = c0.w;
+                    cin[4] = c1.x, cin[5] = c1.y, cin[6] = c1.z, cin[7] = c1.w;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) cin[j] = 1.0f;
+                }
+                float v[8];
                 __syncwarp();
-                tmem_ld16(acc + 16u * g, v);
-                const int k0 = kbase + 16 * g;
-                if (!in_row || k0 >= Mout) continue;
-                if (S64) {
+                tmem_ld8(last_acc + (uint32_t)e0, v);
+                if (!live_k) continue;
+                float snew[8];
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (k0 + j < Mout)
-                            S64[(int64_t)(k0 + j) * Nc] =
-                                (double)(bterm + lam * (v[j] * rinv * (fp16 ? __ldg(cs_inv + k0 + j) : 1.0f)));
+                for (int j = 0; j < 8; ++j) snew[j] = fmaf(v[j] * cin[j], lr, bterm);
+                if (S64) {
+                    double* dp = S64 + (int64_t)k0 * Nc;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j, dp += Nc)
+                        if (j < nk) *dp = (double)snew[j];
                     continue;
                 }
-                const uint16_t* ph = reinterpret_cast<const uint16_t*>(rh);
-                const uint16_t* pl = reinterpret_cast<const uint16_t*>(rl);
-                uint16_t nh[16], nl[16];
-                const bool do_relax = relax && k0 < kpad;
+                {
+                    float* sp = S + (int64_t)k0 * Nc;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int k = k0 + j;
-                    float xnext = 0.0f;
-                    if (k < Mout) {
-                        const float cinv = fp16 ? __ldg(cs_inv + k) : 1.0f;
-                        const float snew = bterm + lam * (v[j] * rinv * cinv);
-                        if (residual) rmax = fmaxf(rmax, fabsf(snew - old[j]));
-                        S[(int64_t)k * Nc] = snew;
-                        if (do_relax) xnext = 0.5f * join_any(fp16, ph[j], pl[j]) + 0.5f * (snew * rsc);
-                    }
-                    if (do_relax) {
-                        if (fp16 && fabsf(xnext) > 60000.0f) overflow = true;
-                        split_any(fp16, xnext, nh[j], nl[j]);
-                    }
+                    for (int j = 0; j < 8; ++j, sp += Nc)
+                        if (j < nk) {
+                            *sp = snew[j];
+                            rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
+                        }
                 }
                 if (do_relax) {
+                    const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
+                    const uint32_t lw[4] = {rl.x, rl.y, rl.z, rl.w};
+                    uint32_t nh[4], nl[4];  // new split pairs, packed as they are made
+#pragma unroll
+                    for (int j = 0; j < 8; j += 2) {
+                        uint16_t h2[2], l2[2];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const uint16_t ho = (uint16_t)(hw[j >> 1] >> (16 * u));
+                            const uint16_t lo = (uint16_t)(lw[j >> 1] >> (16 * u));
+                            // columns past Mout stay zero (the padding of the split rows)
+                            const float x = (j + u < nk) ? fmaf(snew[j + u], hrsc, 0.5f * join_any(fp16, ho, lo)) : 0.0f;
+                            if (fp16 && fabsf(x) > 60000.0f) overflow = true;
+                            split_any(fp16, x, h2[u], l2[u]);
+                        }
+                        nh[j >> 1] = pack2(h2[0], h2[1]);
+                        nl[j >> 1] = pack2(l2[0], l2[1]);
+                    }
                     uint4* dst = reinterpret_cast<uint4*>(nrow + rts_ptx::ilv_hi(k0));
-                    dst[0] = make_uint4(pack2(nh[0], nh[1]), pack2(nh[2], nh[3]), pack2(nh[4], nh[5]), pack2(nh[6], nh[7]));
-                    dst[1] = make_uint4(pack2(nh[8], nh[9]), pack2(nh[10], nh[11]), pack2(nh[12], nh[13]),
-                                        pack2(nh[14], nh[15]));
-                    dst[4] = make_uint4(pack2(nl[0], nl[1]), pack2(nl[2], nl[3]), pack2(nl[4], nl[5]), pack2(nl[6], nl[7]));
-                    dst[5] = make_uint4(pack2(nl[8], nl[9]), pack2(nl[10], nl[11]), pack2(nl[12], nl[13]),
-                                        pack2(nl[14], nl[15]));
+                    dst[0] = make_uint4(nh[0], nh[1], nh[2], nh[3]);
+                    dst[4] = make_uint4(nl[0], nl[1], nl[2], nl[3]);
                 }
             }
-#undef RTS_EPI_LOAD
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty_bar((int)((ch - 1) & 1)));
+            release_last();
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
                 if (lane == 0 && rmax > 0.0f)
-                    atomicMax(resid, (unsigned long long)__double_as_longlong((double)rmax));
+                    atomicMax(P.resid, (unsigned long long)__double_as_longlong((double)rmax));
             }
         }
     }
