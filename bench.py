@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--flush", type=int, default=0, choices=[0, 1, 2],
+                    help="tensor-core K-slices per FP32 drain (0: library default, 1)")
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
                     help="2: the headline source iteration (default); 1, 3, 4, 5: the other configurations")
     return ap.parse_args()
@@ -291,6 +293,8 @@ def run_ours(args, rank, world, local):
     B = _native.synth_uniform(WORKLOAD["seed"], 2, 0.1, 1.0, N)
     ctx = pkg.Context(local)
     ctx.init(xyz, area, fa, N)
+    if args.flush:
+        ctx.set_tuning(_native.TUNE_FLUSH, args.flush)
 
     def fresh(precision):
         ctx.synth_illum(WORKLOAD["seed"], WORKLOAD["mu"], WORKLOAD["sigma"])
@@ -420,6 +424,7 @@ def run_ours(args, rank, world, local):
         "ms_per_step": elapsed / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": dtype, "data": "synthetic",
         "config": {"workload": WORKLOAD["name"], "cells": N, "dirs": M, "precision": prec,
+                   "flush": args.flush or 1,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (no flush)", "step": "integral + update + residual + relaxation"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,

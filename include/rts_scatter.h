@@ -395,8 +395,15 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
 /* Tuning knobs of the tensor-core path (0 restores the default):
  *   RTS_TUNE_FLUSH: in-direction blocks of 32 (1 or 2) accumulated on the
  *   tensor core before the partial sum is added in FP32 on the CUDA cores
- *   (default 1; 1 is more accurate, 2 issues half as many drains). */
+ *   (default 1; 1 is more accurate, 2 issues half as many drains).
+ *   RTS_TUNE_BIAS: correction of the tensor core's truncating FP32
+ *   accumulation.  Each accumulate rounds toward zero, so every partial sum
+ *   comes out low by a fixed fraction on average (about 1e-7 relative per
+ *   evaluation, measured per precision and flush period); the tensor paths
+ *   scale the finished sums by (1 + that fraction).  0 = the measured
+ *   default, -1 = no correction, n > 0 = a custom fraction of n * 1e-10. */
 #define RTS_TUNE_FLUSH 1
+#define RTS_TUNE_BIAS 2
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* The cudaStream_t of a stream slot (for callers that order their own work

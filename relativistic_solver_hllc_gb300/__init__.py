@@ -16,6 +16,8 @@ from ._native import (  # noqa: F401
     STREAM_PARAMS,
     STREAM_SCATTERING_1,
     STREAM_SCATTERING_2,
+    TUNE_BIAS,
+    TUNE_FLUSH,
     Batch,
     Context,
     RtsError,

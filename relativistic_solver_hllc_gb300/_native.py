@@ -58,6 +58,9 @@ class RtsError(RuntimeError):
         super().__init__(f"{where}: {name}" + (f": {message}" if message else ""))
 
 
+TUNE_FLUSH = 1  # RTS_TUNE_FLUSH
+TUNE_BIAS = 2   # RTS_TUNE_BIAS
+
 _dp = C.POINTER(C.c_double)
 _i64 = C.c_int64
 _vp = C.c_void_p

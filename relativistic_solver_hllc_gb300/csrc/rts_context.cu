@@ -696,6 +696,11 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
                     "flush period %d outside [0, 2]", value);
         ctx->split_flush = value;
         return RTS_OK;
+    case RTS_TUNE_BIAS:
+        RTS_REQUIRE(ctx, value >= -1, RTS_ERR_INVALID_ARGUMENT, "bias correction %d below -1", value);
+        ctx->split_bias = value;
+        ctx->tuning_epoch++;  // batch tables are rebuilt at their next step or capture
+        return RTS_OK;
     default:
         return rts_fail(ctx, RTS_ERR_INVALID_ARGUMENT, "unknown tuning key %d", key);
     }

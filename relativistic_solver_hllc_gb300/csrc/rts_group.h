@@ -57,3 +57,4 @@ rts_ctx* rts_group_ctx(rts_batch* b);
 // Forces the device table to be rebuilt before the next launch (after the
 // caller changed cur / S64 / use_B of a problem) and drops a captured graph.
 void rts_group_invalidate(rts_batch* b);
+float rts_group_bias(const rts_ctx* ctx, bool fp16, int flush);

@@ -62,6 +62,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     int m_tiles, n_tiles;
     int Mout, kpad, kblocks, bn, flush, groups;
     uint32_t idesc;
+    float bias;           // relative correction of the truncation bias of the sums
     int fp16;
     int cur;              // buffer holding the current Ibar
     int relax, residual;
@@ -317,6 +318,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float lr = lam * ((fp16 && in_row) ? P.rs_inv[r] : 1.0f);
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
+            const float bias = P.bias;
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * Nc + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * Nc + cc : nullptr;
             const int cur = P.cur;
@@ -363,7 +365,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 if (!live_k) continue;
                 float snew[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) snew[j] = fmaf(v[j] * cin[j], lr, bterm);
+                for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
                 if (S64) {
                     double* dp = S64 + (int64_t)k0 * Nc;
 #pragma unroll

@@ -94,6 +94,8 @@ struct rts_ctx {
     int64_t solve_steps = 0;
     rts_split_state split;
     int split_flush = 0;         // hi*hi drain period in stages (0: default)
+    int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
+    int tuning_epoch = 0;        // bumped when a setting that batch tables copy changes
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context

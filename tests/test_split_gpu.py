@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
-from relativistic_solver_hllc_gb300 import PHASE_HG
+from relativistic_solver_hllc_gb300 import PHASE_HG, TUNE_BIAS
 
 pytestmark = pytest.mark.gpu
 TOL = {"fp16x3": 1e-6, "bf16x3": 2e-5}
@@ -67,11 +67,41 @@ def test_source_iteration_with_relaxation(ctx, prec):
     W = oracle.weights_thomson(xyz, area, fa)
     S_ref, r_ref, I_ref = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
     # errors of successive steps compound through a contraction of norm <= 0.95
-    assert rel_err(S, S_ref) <= 4 * TOL[prec]
+    assert rel_err(S, S_ref) <= (1 if prec == "fp16x3" else 4) * TOL[prec]
     assert rel_err(np.array(res[1:]), r_ref[1:]) <= 1e-2
     assert rel_err(ctx.solve_read_ibar(), I_ref) <= 4 * TOL[prec]
     hist = ctx.solve_residual_history(iters)
     assert np.allclose(hist, res, rtol=0, atol=0)
+
+
+def test_truncation_bias_correction(ctx):
+    """tcgen05.mma rounds every FP32 accumulate toward zero, so uncorrected
+    sums come out low and the loss compounds through a relaxed iteration; the
+    calibrated correction (RTS_TUNE_BIAS default) removes most of it."""
+    N, M, lam, iters = 2048, 384, 0.9, 8
+    xyz, area, fa, il, B = problem(N, M, seed=4, sigma=1.5)
+    W = oracle.weights_thomson(xyz, area, fa)
+    S_ref, _, _ = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
+    ctx.init(xyz, area, fa, N)
+    stats = {}
+    try:
+        for mode in (-1, 0):
+            ctx.set_tuning(TUNE_BIAS, mode)
+            ctx.copy_illum(il)
+            ctx.solve_setup("fp16x3", B, lam)
+            for _ in range(iters):
+                ctx.solve_step_async(True)
+            ctx.wait()
+            d = (ctx.solve_read() - S_ref) / S_ref
+            stats[mode] = (float(d.mean()), float(np.abs(d).max()))
+    finally:
+        ctx.set_tuning(TUNE_BIAS, 0)
+    off, on = stats[-1], stats[0]
+    assert off[0] < -1e-7  # truncation loses
+    assert abs(on[0]) < 0.5 * abs(off[0])
+    assert on[1] <= TOL["fp16x3"]
+    with pytest.raises(Exception):
+        ctx.set_tuning(TUNE_BIAS, -2)
 
 
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
