@@ -253,6 +253,7 @@ int rts_init(rts_ctx* ctx, const double* xyz, const double* area, int64_t M, dou
     RTS_CUDA_TRY(ctx, cudaMemcpy(ctx->d_xyz, xyz, rts_bytes<double>(M * 3), cudaMemcpyHostToDevice));
     RTS_CUDA_TRY(ctx, cudaMemcpy(ctx->d_area, area, rts_bytes<double>(M), cudaMemcpyHostToDevice));
     RTS_CUDA_TRY(ctx, cudaMemset(ctx->d_S, 0, rts_bytes<double>(loc * N)));
+    ctx->w_version++;
     return rts_launch_weights(ctx);
 }
 
@@ -283,6 +284,7 @@ int rts_set_phase(rts_ctx* ctx, int phase, double g)
     ctx->phase = phase;
     ctx->phase_g = g;
     ctx->solve_ready = false;
+    ctx->w_version++;
     return rts_launch_weights(ctx);
 }
 
@@ -295,6 +297,7 @@ int rts_set_weights(rts_ctx* ctx, const double* W)
                                  cudaMemcpyHostToDevice));
     ctx->phase = RTS_PHASE_CUSTOM;
     ctx->solve_ready = false;
+    ctx->w_version++;
     return RTS_OK;
 }
 
@@ -398,6 +401,11 @@ int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
                 "rts_scattering_update: null host buffer");
     RTS_REQUIRE(ctx, B_host || lambda == 1.0, RTS_ERR_INVALID_ARGUMENT,
                 "rts_scattering_update: B is required unless lambda == 1");
+    if (precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3) {
+        ctx->solve_ready = false;
+        return rts_split_host_call(ctx, precision, illum_host, B_host, lambda, S_host);
+    }
+    RTS_REQUIRE(ctx, precision == RTS_PREC_FP64, RTS_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_illum, illum_host,
                                       rts_bytes<double>(ctx->M * ctx->N * 4),
@@ -407,14 +415,7 @@ int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
     if (update)
         RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_B, B_host, rts_bytes<double>(ctx->N),
                                           cudaMemcpyHostToDevice, st));
-    int rc;
-    if (precision == RTS_PREC_FP64) {
-        rc = rts_launch_scatter_fp64(ctx, 0, ctx->local(), st, ctx->d_B, lambda, update, false);
-    } else if (precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3) {
-        rc = rts_split_oneshot(ctx, precision, update ? ctx->d_B : nullptr, lambda, st);
-    } else {
-        return rts_fail(ctx, RTS_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
-    }
+    int rc = rts_launch_scatter_fp64(ctx, 0, ctx->local(), st, ctx->d_B, lambda, update, false);
     if (rc != RTS_OK) return rc;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(S_host, ctx->d_S, rts_bytes<double>(ctx->local() * ctx->N),
                                       cudaMemcpyDeviceToHost, st));

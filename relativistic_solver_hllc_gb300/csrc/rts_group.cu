@@ -313,6 +313,7 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
         memcpy(&g.mapA[1], p->maps[1], 128);
         memcpy(&g.mapW, p->maps[2], 128);
         g.N = p->N;
+        g.ldS = p->ldS > 0 ? p->ldS : p->N;
         g.rows = p->rows;
         g.tile_begin = tiles;
         g.m_tiles = (int)p->m_tiles;
@@ -352,6 +353,14 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
     b->table_relax = relax;
     b->table_epoch = ctx->tuning_epoch;
     return RTS_OK;
+}
+
+int rts_group_prepare(rts_batch* b, int relax, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    if (b->probs.empty()) return RTS_OK;
+    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    return upload_table(b, relax, st);
 }
 
 static int enqueue_step(rts_batch* b, int relax, cudaStream_t st)

@@ -26,7 +26,8 @@ struct GProb {
     float* B = nullptr;      // [rows]
     float* lam = nullptr;    // [groups]
     float* S32 = nullptr;    // [groups][Mout][N] (source iteration)
-    double* S64 = nullptr;   // [groups][Mout][N] FP64 output (host-buffer calls), not owned
+    double* S64 = nullptr;   // [groups][Mout][ldS] FP64 output (host-buffer calls), not owned
+    int64_t ldS = 0;         // row pitch of the S output in cells (0: N)
     bool use_B = true;       // false: the bare integral (no source update)
     int cur = 0;
     int slot = -1;           // index of the problem's residual in the last launched table
@@ -45,6 +46,9 @@ int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
 GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
 int rts_group_remove(rts_batch* b, int64_t id);
 int rts_group_step(rts_batch* b, int relax, cudaStream_t st);
+// Builds and uploads the device table now (a later step of an unchanged batch
+// then queues its launch without a host synchronisation).
+int rts_group_prepare(rts_batch* b, int relax, cudaStream_t st);
 int rts_group_capture(rts_batch* b, int steps, int relax);
 int rts_group_replay(rts_batch* b);
 int64_t rts_group_total_tiles(rts_batch* b);

@@ -57,6 +57,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     CUtensorMap mapA[2];  // split Ibar, ping-pong buffers
     CUtensorMap mapW;     // split W^T
     int64_t N;            // cells per group
+    int64_t ldS;          // row pitch of S32 / S64 in cells (>= N; N unless the output is a cell range of a wider S)
     int64_t rows;         // groups * N
     int64_t tile_begin;   // first global tile index of this problem
     int m_tiles, n_tiles;
@@ -257,13 +258,13 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     if (c == (nchunks >> 1) && ncols > 0) {
                         const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
                         if (r < P.rows) {
-                            const int64_t Nc = P.N;
+                            const int64_t Nc = P.N, ld = P.ldS;
                             const int Mout = P.Mout, kb0 = n_tile * bn + 64 * cs;
                             const int64_t grp = r / Nc;
                             if (P.S32 && P.residual) {
-                                const float* Sp = P.S32 + grp * (int64_t)Mout * Nc + (r - grp * Nc);
+                                const float* Sp = P.S32 + grp * (int64_t)Mout * ld + (r - grp * Nc);
                                 for (int j = 0; j < ncols && kb0 + j < Mout; ++j)
-                                    prefetch_l2(Sp + (int64_t)(kb0 + j) * Nc);
+                                    prefetch_l2(Sp + (int64_t)(kb0 + j) * ld);
                             }
                             if (P.relax && P.S32 && !P.S64 && kb0 < P.kpad) {
                                 const uint16_t* ar = P.a[P.cur] + r * 2 * (int64_t)P.kpad;
@@ -305,7 +306,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             //   S = (1 - lam) B + lam * rs_inv[row] * cs_inv[k] * acc
             //   Ibar' = 0.5 Ibar + 0.5 rs[row] * S   (relaxation, split again)
             const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
-            const int64_t Nc = P.N;
+            const int64_t Nc = P.N, ld = P.ldS;
             const int Mout = P.Mout, kpad = P.kpad;
             const bool in_row = r < P.rows;
             const int64_t grp = in_row ? r / Nc : 0;
@@ -319,8 +320,8 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
             const float bias = P.bias;
-            float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * Nc + cc : nullptr;
-            double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * Nc + cc : nullptr;
+            float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
+            double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             const int cur = P.cur;
             const uint16_t* __restrict__ arow = P.a[cur] + r * 2 * (int64_t)kpad;
             uint16_t* __restrict__ nrow = P.a[cur ^ 1] + r * 2 * (int64_t)kpad;
@@ -336,9 +337,9 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 // global loads first, then the TMEM read
                 float old[8];
                 if (live_k && residual && S) {
-                    const float* sp = S + (int64_t)k0 * Nc;
+                    const float* sp = S + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, sp += Nc) old[j] = j < nk ? *sp : 0.0f;
+                    for (int j = 0; j < 8; ++j, sp += ld) old[j] = j < nk ? *sp : 0.0f;
                 } else {
 #pragma unroll
                     for (int j = 0; j < 8; ++j) old[j] = 0.0f;
@@ -367,16 +368,16 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
 #pragma unroll
                 for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
                 if (S64) {
-                    double* dp = S64 + (int64_t)k0 * Nc;
+                    double* dp = S64 + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, dp += Nc)
+                    for (int j = 0; j < 8; ++j, dp += ld)
                         if (j < nk) *dp = (double)snew[j];
                     continue;
                 }
                 {
-                    float* sp = S + (int64_t)k0 * Nc;
+                    float* sp = S + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, sp += Nc)
+                    for (int j = 0; j < 8; ++j, sp += ld)
                         if (j < nk) {
                             *sp = snew[j];
                             rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));

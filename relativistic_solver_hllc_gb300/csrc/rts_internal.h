@@ -41,13 +41,20 @@ constexpr int64_t RTS_RESID_CAP = 4096;
 
 // Split-precision operands of one source iteration (tensor-core path).
 struct rts_batch;
+constexpr int RTS_HOST_CHUNKS = 8;  // cell ranges of a pipelined host-buffer call
+
 struct rts_split_state {
     int precision = -1;             // precision of the resident source iteration
     rts_batch* iter = nullptr;      // one-problem batch of the source iteration
     int64_t iter_id = 0;
-    int shot_precision = -1;        // precision of the host-buffer problem
-    rts_batch* shot = nullptr;      // one-problem batch of host-buffer calls (FP64 S out)
-    int64_t shot_id = 0;
+    // host-buffer calls: one one-problem batch per cell range, pipelined
+    // (copy in on `copy_in`, split + contraction on the scattering stream,
+    // copy out on `copy_out`)
+    rts_batch* chunk[RTS_HOST_CHUNKS] = {};
+    int64_t chunk_id[RTS_HOST_CHUNKS] = {};
+    int64_t chunk_w_version[RTS_HOST_CHUNKS] = {};
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_in[RTS_HOST_CHUNKS] = {}, ev_done[RTS_HOST_CHUNKS] = {};
 };
 
 struct rts_ctx {
@@ -96,6 +103,7 @@ struct rts_ctx {
     int split_flush = 0;         // hi*hi drain period in stages (0: default)
     int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
     int tuning_epoch = 0;        // bumped when a setting that batch tables copy changes
+    int64_t w_version = 0;       // bumped whenever d_W is rewritten
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context
@@ -130,7 +138,7 @@ int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_ar
 // Operand preparation of the split-precision path (rts_prepass.cu).
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, bool fp16,
                    uint16_t* Wc, float* cs, cudaStream_t st);
-int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int M, int kpad, const double* B, bool fp16,
+int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B, bool fp16,
                            float* rs, int64_t npad, uint16_t* A, cudaStream_t st);
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
                          bool fp16, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st);
@@ -144,7 +152,8 @@ int rts_split_setup(rts_ctx* ctx, int precision);
 int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
 // One evaluation from the device Illum (faces) into the FP64 device S, with
 // the source update when B != nullptr; local out-directions [0, local).
-int rts_split_oneshot(rts_ctx* ctx, int precision, const double* B, double lambda, cudaStream_t st);
+int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, const double* B_host, double lambda,
+                        double* S_host);
 int rts_split_read(rts_ctx* ctx, double* S_host);
 int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host);
 void rts_split_free(rts_ctx* ctx);

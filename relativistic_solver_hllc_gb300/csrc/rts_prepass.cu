@@ -72,8 +72,9 @@ __device__ __forceinline__ double face_mean(const double* __restrict__ illum, in
     return I / 4;
 }
 
-// Row scales from the face layout: thread per cell.
-__global__ void rowscale_faces_kernel(const double* __restrict__ illum, int64_t N, int M,
+// Row scales from the face layout: thread per cell.  The N cells are columns
+// of an Illum whose rows hold `ld` cells (a cell range of a wider Illum).
+__global__ void rowscale_faces_kernel(const double* __restrict__ illum, int64_t N, int64_t ld, int M,
                                       const double* __restrict__ B, float* __restrict__ rs, int64_t npad)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,7 +82,7 @@ __global__ void rowscale_faces_kernel(const double* __restrict__ illum, int64_t 
     float s = 1.0f;
     if (c < N) {
         double m = B ? fabs(B[c]) : 0.0;
-        for (int j = 0; j < M; ++j) m = fmax(m, fabs(face_mean(illum, N, j, c)));
+        for (int j = 0; j < M; ++j) m = fmax(m, fabs(face_mean(illum, ld, j, c)));
         s = pow2_scale(2.0 * m);
     }
     rs[c] = s;
@@ -164,11 +165,11 @@ struct F32Src {
     }
 };
 
-__global__ void __launch_bounds__(256) split_faces_kernel(const double* __restrict__ illum, int64_t N, int M, int kpad,
-                                                          const float* __restrict__ rs, int fp16,
+__global__ void __launch_bounds__(256) split_faces_kernel(const double* __restrict__ illum, int64_t N, int64_t ld,
+                                                          int M, int kpad, const float* __restrict__ rs, int fp16,
                                                           uint16_t* __restrict__ A)
 {
-    split_tile(FacesSrc{illum, N}, N, M, kpad, rs, fp16, A);
+    split_tile(FacesSrc{illum, ld}, N, M, kpad, rs, fp16, A);
 }
 
 __global__ void __launch_bounds__(256) split_f32_kernel(const float* __restrict__ ibar, int64_t N, int M,
@@ -225,16 +226,16 @@ int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, in
     return RTS_OK;
 }
 
-int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int M, int kpad, const double* B, bool fp16,
-                           float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
+int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B,
+                           bool fp16, float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
 {
     if (fp16) {
-        rowscale_faces_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(illum, N, M, B, rs, npad);
+        rowscale_faces_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(illum, N, ld, M, B, rs, npad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_faces_kernel");
         ctx->launches++;
     }
     dim3 grid((unsigned)((N + 63) / 64), (unsigned)(kpad / 32));
-    split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, M, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
+    split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, ld, M, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
     RTS_CHECK_LAUNCH(ctx, "split_faces_kernel");
     ctx->launches++;
     return RTS_OK;

@@ -7,6 +7,7 @@
 //
 // Reference counterpart: d_GetS_MPI_Stream (cuda/cuda_kernel.cu:82-111) and
 // its launch in CalculateIntScatteringAsyncMPIStream (cuda/cuda_solve.cu:89-111).
+#include <algorithm>
 #include <cstring>
 
 #include "rts_group.h"
@@ -48,7 +49,7 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
     p->cur = 0;
     p->S64 = S64;
     p->use_B = B_dev != nullptr;
-    int rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, (int)Min, (int)p->kpad, B_dev, fp16, p->rs, p->rows_pad,
+    int rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)Min, (int)p->kpad, B_dev, fp16, p->rs, p->rows_pad,
                                     p->a[0], st);
     if (rc != RTS_OK) return rc;
     if (B_dev) {
@@ -90,13 +91,138 @@ int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st)
     return RTS_OK;
 }
 
-int rts_split_oneshot(rts_ctx* ctx, int precision, const double* B, double lambda, cudaStream_t st)
+namespace {
+
+int ensure_pipeline(rts_ctx* ctx)
+{
+    rts_split_state& s = ctx->split;
+    if (s.copy_in) return RTS_OK;
+    RTS_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s.copy_in, cudaStreamNonBlocking));
+    RTS_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s.copy_out, cudaStreamNonBlocking));
+    RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&s.ev_start, cudaEventDisableTiming));
+    for (int i = 0; i < RTS_HOST_CHUNKS; ++i) {
+        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&s.ev_in[i], cudaEventDisableTiming));
+        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&s.ev_done[i], cudaEventDisableTiming));
+    }
+    return RTS_OK;
+}
+
+// The one-problem batch of cell range i with n cells, rebuilt when its shape,
+// precision or flush period changed; W split again when the context's W did.
+int chunk_problem(rts_ctx* ctx, int i, int64_t n, bool fp16, int flush, GProb** out, cudaStream_t st)
+{
+    rts_split_state& s = ctx->split;
+    const int64_t M = ctx->M, Mout = ctx->local();
+    int rc;
+    GProb* p = s.chunk[i] ? rts_group_find(s.chunk[i], s.chunk_id[i], nullptr) : nullptr;
+    if (p && (p->fp16 != fp16 || p->N != n || p->M != M || p->Mout != Mout || p->flush != flush)) {
+        if ((rc = rts_group_remove(s.chunk[i], s.chunk_id[i])) != RTS_OK) return rc;
+        p = nullptr;
+    }
+    if (!s.chunk[i] && (rc = rts_group_batch_new(ctx, &s.chunk[i])) != RTS_OK) return rc;
+    if (!p) {
+        rc = rts_group_new_problem(s.chunk[i], n, M, Mout, 1, ctx->d_W, (int)Mout, fp16, flush, 0, false, &p);
+        if (rc != RTS_OK) return rc;
+        if ((rc = rts_group_attach(s.chunk[i], p, &s.chunk_id[i])) != RTS_OK) return rc;
+        s.chunk_w_version[i] = ctx->w_version;
+    } else if (s.chunk_w_version[i] != ctx->w_version) {
+        rc = rts_pp_split_w(ctx, ctx->d_W, (int)M, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, fp16, p->wc, p->cs,
+                            st);
+        if (rc != RTS_OK) return rc;
+        s.chunk_w_version[i] = ctx->w_version;
+    }
+    *out = p;
+    return RTS_OK;
+}
+
+}  // namespace
+
+// rts_scattering_update at FP16x3 / BF16x3, pipelined over cell ranges.
+// Row c of S depends only on row c of Ibar, so the N cells are cut into up
+// to RTS_HOST_CHUNKS ranges; range i is copied in (one strided 2-D copy of
+// its columns of the [M][N][4] host Illum), split and contracted on the
+// scattering stream, and copied out (strided 2-D copy of its columns of the
+// [local][N] S), so the H2D of one range, the compute of the previous one
+// and the D2H of the one before run at the same time.  The device copy of
+// Illum ends up complete, as after the reference's CalculateIntScattering.
+int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, const double* B_host, double lambda,
+                        double* S_host)
 {
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
-    int rc = build_problem(ctx, &ctx->split.shot, &ctx->split.shot_id, precision, false, B, lambda, ctx->d_S, st);
+    int rc = ensure_pipeline(ctx);
     if (rc != RTS_OK) return rc;
-    ctx->split.shot_precision = precision;
-    return rts_group_step(ctx->split.shot, 0, st);
+    rts_split_state& s = ctx->split;
+    const bool fp16 = precision == RTS_PREC_FP16X3;
+    const bool update = B_host != nullptr && lambda != 1.0;
+    const int64_t N = ctx->N, M = ctx->M, Mout = ctx->local();
+    const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
+    const int64_t tiles = (N + 127) / 128;
+    const int nch = (int)std::min<int64_t>(RTS_HOST_CHUNKS, tiles);
+    const int64_t csz = (tiles + nch - 1) / nch * 128;  // cells per range, whole 128-cell tiles
+    cudaStream_t sc = ctx->streams[RTS_STREAM_SCATTERING_1];
+    const float lamf = (float)lambda;
+
+    // set-up (host-synchronous, before any copy is queued)
+    GProb* probs[RTS_HOST_CHUNKS] = {};
+    int used = 0;
+    for (int i = 0; i < nch; ++i) {
+        const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
+        if (n <= 0) break;
+        GProb* p = nullptr;
+        if ((rc = chunk_problem(ctx, i, n, fp16, flush, &p, sc)) != RTS_OK) return rc;
+        const bool changed = p->S64 != ctx->d_S + c0 || p->ldS != N || p->use_B != update || p->cur != 0;
+        p->cur = 0;
+        p->S64 = ctx->d_S + c0;
+        p->ldS = N;
+        p->use_B = update;
+        if (update) RTS_CUDA_TRY(ctx, cudaMemcpyAsync(p->lam, &lamf, sizeof(float), cudaMemcpyHostToDevice, sc));
+        if (changed) rts_group_invalidate(s.chunk[i]);
+        if ((rc = rts_group_prepare(s.chunk[i], 0, sc)) != RTS_OK) return rc;
+        probs[used++] = p;
+    }
+    RTS_CUDA_TRY(ctx, cudaStreamSynchronize(sc));  // the host lambda must outlive its copies
+
+    auto drain = [&]() {
+        cudaStreamSynchronize(s.copy_in);
+        cudaStreamSynchronize(sc);
+        cudaStreamSynchronize(s.copy_out);
+    };
+    RTS_CUDA_TRY(ctx, cudaEventRecord(s.ev_start, sc));
+    RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(s.copy_in, s.ev_start, 0));
+    RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(s.copy_out, s.ev_start, 0));
+    for (int i = 0; i < used && rc == RTS_OK; ++i) {
+        GProb* p = probs[i];
+        const int64_t c0 = i * csz, n = p->N;
+        cudaError_t e = cudaMemcpy2DAsync(ctx->d_illum + c0 * 4, (size_t)N * 32, illum_host + c0 * 4, (size_t)N * 32,
+                                          (size_t)n * 32, (size_t)M, cudaMemcpyHostToDevice, s.copy_in);
+        if (e == cudaSuccess && update)
+            e = cudaMemcpyAsync(ctx->d_B + c0, B_host + c0, (size_t)n * 8, cudaMemcpyHostToDevice, s.copy_in);
+        if (e == cudaSuccess) e = cudaEventRecord(s.ev_in[i], s.copy_in);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sc, s.ev_in[i], 0);
+        if (e != cudaSuccess) {
+            rc = rts_fail(ctx, RTS_ERR_CUDA, "host-call copy in: %s", cudaGetErrorString(e));
+            break;
+        }
+        rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad,
+                                    update ? ctx->d_B + c0 : nullptr, fp16, p->rs, p->rows_pad, p->a[0], sc);
+        if (rc == RTS_OK && update) rc = rts_pp_f64_to_f32(ctx, ctx->d_B + c0, p->B, n, sc);
+        if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, sc);
+        if (rc != RTS_OK) break;
+        e = cudaEventRecord(s.ev_done[i], sc);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s.copy_out, s.ev_done[i], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(S_host + c0, (size_t)N * 8, ctx->d_S + c0, (size_t)N * 8, (size_t)n * 8,
+                                  (size_t)Mout, cudaMemcpyDeviceToHost, s.copy_out);
+        if (e != cudaSuccess) rc = rts_fail(ctx, RTS_ERR_CUDA, "host-call copy out: %s", cudaGetErrorString(e));
+    }
+    drain();
+    if (rc != RTS_OK) return rc;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return rts_fail(ctx, RTS_ERR_CUDA, "host call: %s", cudaGetErrorString(e));
+    int flag = 0;
+    RTS_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return rts_fail(ctx, RTS_ERR_DEVICE_WAIT, "tensor-path kernel reported device flag %d", flag);
+    return RTS_OK;
 }
 
 int rts_split_read(rts_ctx* ctx, double* S_host)
@@ -133,7 +259,15 @@ int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host)
 
 void rts_split_free(rts_ctx* ctx)
 {
-    rts_group_batch_free(ctx->split.iter);
-    rts_group_batch_free(ctx->split.shot);
-    ctx->split = rts_split_state();
+    rts_split_state& s = ctx->split;
+    rts_group_batch_free(s.iter);
+    for (int i = 0; i < RTS_HOST_CHUNKS; ++i) {
+        rts_group_batch_free(s.chunk[i]);
+        if (s.ev_in[i]) cudaEventDestroy(s.ev_in[i]);
+        if (s.ev_done[i]) cudaEventDestroy(s.ev_done[i]);
+    }
+    if (s.ev_start) cudaEventDestroy(s.ev_start);
+    if (s.copy_in) cudaStreamDestroy(s.copy_in);
+    if (s.copy_out) cudaStreamDestroy(s.copy_out);
+    s = rts_split_state();
 }

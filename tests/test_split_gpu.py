@@ -119,6 +119,29 @@ def test_host_buffer_entry_point(ctx, prec):
     assert rel_err(out.reshape(M, N), oracle.calculate_int_cpu(N, xyz, area, fa, il)) <= TOL[prec]
 
 
+def test_host_buffer_call_pipelined_over_cell_ranges(ctx):
+    """The tensor-precision host call runs over up to 8 cell ranges (ragged
+    tail here); the result, the device copy of Illum and a change of W between
+    calls (Thomson -> HG: the split W is refreshed) must all come out right."""
+    N, M, lam = 128 * 8 * 3 + 77, 64, 0.8
+    xyz, area, fa, il, B = problem(N, M, seed=8, indep=True)
+    ctx.init(xyz, area, fa, N)
+    pinned = ctx.host_illum()
+    pinned[:] = il.reshape(-1)
+    out = np.zeros(M * N)
+    ctx.scattering_update("fp16x3", pinned, B, lam, out)
+    ref = oracle.source_update(oracle.calculate_int_cpu(N, xyz, area, fa, il), B, lam)
+    assert rel_err(out.reshape(M, N), ref) <= TOL["fp16x3"]
+    back = np.zeros_like(pinned)
+    ctx.read_illum(back)
+    assert np.array_equal(back, pinned)
+    ctx.set_phase(PHASE_HG, 0.5)
+    ctx.scattering_update("fp16x3", il, B, lam, out)  # pageable host buffers this time
+    ref64 = np.zeros(M * N)
+    ctx.scattering_update("fp64", il, B, lam, ref64)
+    assert rel_err(out, ref64) <= TOL["fp16x3"]
+
+
 def test_shard_of_out_directions_tensor(ctx):
     N, M = 400, 80
     xyz, area, fa, il, B = problem(N, M, seed=4)
