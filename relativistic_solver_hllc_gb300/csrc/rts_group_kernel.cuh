@@ -50,7 +50,10 @@ constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
 constexpr int G_CTAS_PER_SM = 1;
 constexpr uint32_t G_TMEM_COLS = 512;
 constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
-constexpr size_t G_SMEM = (size_t)G_STAGES * G_STAGE_BYTES + 1024 + 256;
+constexpr int G_BAR_BYTES = 256;
+constexpr int G_REL_BUF = 2 * 32 * 32;  // per epilogue warp: 2 buffers x 32 rows x (16 B hi + 16 B lo)
+constexpr size_t G_REL_OFF = (size_t)G_STAGES * G_STAGE_BYTES + G_BAR_BYTES;
+constexpr size_t G_SMEM = G_REL_OFF + (size_t)G_EPI_WARPS * G_REL_BUF + 1024;
 static_assert(G_SMEM <= 227 * 1024, "shared memory per CTA");
 
 struct GroupProblem {  // aligned as its CUtensorMap members
@@ -91,13 +94,38 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
     return lo;
 }
 
+// Relaxation of 8 columns of one split row in place (shared memory):
+// Ibar' = 0.5 Ibar + 0.5 * (rs * S), split again into hi + lo; columns at or
+// past `nk` become zero (the padding of the split rows).  Returns true when
+// an FP16 value leaves the range the row scale allows.
+template <bool kFp16>
+__device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk)
+{
+    const uint4 rh = *hp, rl = *lp;
+    const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
+    const uint32_t lw[4] = {rl.x, rl.y, rl.z, rl.w};
+    uint32_t nh[4], nl[4];
+    float amax = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+        const float2 i2 = rts_ptx::join2_any(kFp16, hw[j >> 1], lw[j >> 1]);
+        const float x0 = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * i2.x) : 0.0f;
+        const float x1 = (j + 1 < nk) ? fmaf(snew[j + 1], hrsc, 0.5f * i2.y) : 0.0f;
+        if (kFp16) amax = fmaxf(amax, fmaxf(fabsf(x0), fabsf(x1)));
+        rts_ptx::split2_any(kFp16, x0, x1, nh[j >> 1], nl[j >> 1]);
+    }
+    *hp = make_uint4(nh[0], nh[1], nh[2], nh[3]);
+    *lp = make_uint4(nl[0], nl[1], nl[2], nl[3]);
+    return amax > 60000.0f;
+}
+
 __global__ void __launch_bounds__(G_THREADS, 1)
 group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_tiles, int* flag)
 {
     using namespace rts_ptx;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G_STAGES * G_STAGE_BYTES);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G_STAGES * G_STAGE_BYTES);  // G_BAR_BYTES
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * G_STAGES + 4);
     const uint32_t smem_base = smem_u32(smem);
     const uint32_t bar_base = smem_u32(bars);
@@ -253,9 +281,9 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(acc_empty_bar(a));
-                    // half-way through the tile, pull the epilogue's inputs (the
-                    // previous S and the Ibar rows it relaxes) into L2
-                    if (c == (nchunks >> 1) && ncols > 0) {
+                    // a few chunks before the end of the tile, pull the epilogue's
+                    // inputs (the previous S and the Ibar rows it relaxes) into L2
+                    if (c == max(0, nchunks - 4) && ncols > 0) {
                         const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
                         if (r < P.rows) {
                             const int64_t Nc = P.N, ld = P.ldS;
@@ -322,18 +350,45 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float bias = P.bias;
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
-            const int cur = P.cur;
-            const uint16_t* __restrict__ arow = P.a[cur] + r * 2 * (int64_t)kpad;
-            uint16_t* __restrict__ nrow = P.a[cur ^ 1] + r * 2 * (int64_t)kpad;
             const int kbase = n_tile * bn + 64 * cs;
+            // The relaxation's split rows go through a double buffer per warp in
+            // shared memory, 8 columns (hi 16 B + lo 16 B per row) per step:
+            // the next step's rows are fetched with cp.async while this step
+            // computes, and rows are read and written two lanes per row (rows
+            // are 4*kpad bytes apart: one lane per row would touch 32 lines
+            // per instruction).
+            const bool want_rel = relax && S64 == nullptr;  // relax implies Mout == M <= kpad
+            const int64_t rstride = 4 * (int64_t)kpad;       // bytes per split row
+            const int64_t row0 = (int64_t)m_tile * G_BM + q * 32;
+            const uint8_t* __restrict__ abase = reinterpret_cast<const uint8_t*>(P.a[P.cur]) + row0 * rstride;
+            uint8_t* __restrict__ nbase = reinterpret_cast<uint8_t*>(P.a[P.cur ^ 1]) + row0 * rstride;
+            uint8_t* rbuf = smem + G_REL_OFF + (size_t)(warp - G_EPI_WARP0) * G_REL_BUF;
+            const uint32_t rbuf_s = smem_u32(rbuf);
+            // row rr keeps hi at rr*32 + 16*(rr>>2 & 1) and lo in the other half
+            auto slot = [](int rr, int part) { return rr * 32 + ((part ^ ((rr >> 2) & 1)) << 4); };
+            auto fetch = [&](int e0, int b) {  // rows 16i + lane/2, part lane%2 (0 hi, 1 lo)
+                const int k0 = kbase + e0;
+                if (!want_rel || k0 >= Mout) return;
+                const int64_t boff = (int64_t)(k0 >> 5) * 128 + (k0 & 31) * 2;
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int rr = 16 * i + (lane >> 1), part = lane & 1;
+                    cp_async16(rbuf_s + (uint32_t)(b * (G_REL_BUF / 2) + slot(rr, part)),
+                               abase + rr * rstride + boff + part * 64);
+                }
+            };
             float rmax = 0.0f;
             bool overflow = false;
+            fetch(0, 0);
+            cp_async_commit();
 #pragma unroll 1
-            for (int e0 = 0; e0 < ncols; e0 += 8) {
+            for (int e0 = 0, st = 0; e0 < ncols; e0 += 8, ++st) {
                 const int k0 = kbase + e0;
                 const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
                 const bool live_k = in_row && nk > 0;
-                const bool do_relax = live_k && relax && !S64;  // relax implies Mout == M <= kpad
+                const bool rel = want_rel && nk > 0;  // same for all lanes
+                if (e0 + 8 < ncols) fetch(e0 + 8, (st + 1) & 1);
+                cp_async_commit();
                 // global loads first, then the TMEM read
                 float old[8];
                 if (live_k && residual && S) {
@@ -343,12 +398,6 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 } else {
 #pragma unroll
                     for (int j = 0; j < 8; ++j) old[j] = 0.0f;
-                }
-                uint4 rh = make_uint4(0, 0, 0, 0), rl = make_uint4(0, 0, 0, 0);
-                if (do_relax) {
-                    const uint4* src = reinterpret_cast<const uint4*>(arow + rts_ptx::ilv_hi(k0));
-                    rh = src[0];
-                    rl = src[4];
                 }
                 float cin[8];
                 if (fp16) {
@@ -361,52 +410,51 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     for (int j = 0; j < 8; ++j) cin[j] = 1.0f;
                 }
                 float v[8];
+                cp_async_wait1();
                 __syncwarp();
                 tmem_ld8(last_acc + (uint32_t)e0, v);
-                if (!live_k) continue;
-                float snew[8];
+                uint8_t* rb = rbuf + (st & 1) * (G_REL_BUF / 2);
+                if (live_k) {
+                    float snew[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
-                if (S64) {
-                    double* dp = S64 + (int64_t)k0 * ld;
+                    for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
+                    if (S64) {
+                        double* dp = S64 + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, dp += ld)
-                        if (j < nk) *dp = (double)snew[j];
-                    continue;
-                }
-                {
-                    float* sp = S + (int64_t)k0 * ld;
+                        for (int j = 0; j < 8; ++j, dp += ld)
+                            if (j < nk) *dp = (double)snew[j];
+                    } else {
+                        float* sp = S + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, sp += ld)
-                        if (j < nk) {
-                            *sp = snew[j];
-                            rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
+                        for (int j = 0; j < 8; ++j, sp += ld)
+                            if (j < nk) {
+                                *sp = snew[j];
+                                rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
+                            }
+                        if (rel) {
+                            uint4* hp = reinterpret_cast<uint4*>(rb + slot(lane, 0));
+                            uint4* lp = reinterpret_cast<uint4*>(rb + slot(lane, 1));
+                            if (fp16)
+                                overflow |= relax8<true>(hp, lp, snew, hrsc, nk);
+                            else
+                                relax8<false>(hp, lp, snew, hrsc, nk);
                         }
-                }
-                if (do_relax) {
-                    const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
-                    const uint32_t lw[4] = {rl.x, rl.y, rl.z, rl.w};
-                    uint32_t nh[4], nl[4];  // new split pairs, packed as they are made
-#pragma unroll
-                    for (int j = 0; j < 8; j += 2) {
-                        uint16_t h2[2], l2[2];
-#pragma unroll
-                        for (int u = 0; u < 2; ++u) {
-                            const uint16_t ho = (uint16_t)(hw[j >> 1] >> (16 * u));
-                            const uint16_t lo = (uint16_t)(lw[j >> 1] >> (16 * u));
-                            // columns past Mout stay zero (the padding of the split rows)
-                            const float x = (j + u < nk) ? fmaf(snew[j + u], hrsc, 0.5f * join_any(fp16, ho, lo)) : 0.0f;
-                            if (fp16 && fabsf(x) > 60000.0f) overflow = true;
-                            split_any(fp16, x, h2[u], l2[u]);
-                        }
-                        nh[j >> 1] = pack2(h2[0], h2[1]);
-                        nl[j >> 1] = pack2(l2[0], l2[1]);
                     }
-                    uint4* dst = reinterpret_cast<uint4*>(nrow + rts_ptx::ilv_hi(k0));
-                    dst[0] = make_uint4(nh[0], nh[1], nh[2], nh[3]);
-                    dst[4] = make_uint4(nl[0], nl[1], nl[2], nl[3]);
                 }
+                if (rel) {
+                    // rows outside the problem go back unchanged
+                    __syncwarp();
+                    const int64_t boff = (int64_t)(k0 >> 5) * 128 + (k0 & 31) * 2;
+#pragma unroll
+                    for (int i = 0; i < 2; ++i) {
+                        const int rr = 16 * i + (lane >> 1), part = lane & 1;
+                        *reinterpret_cast<uint4*>(nbase + rr * rstride + boff + part * 64) =
+                            *reinterpret_cast<const uint4*>(rb + slot(rr, part));
+                    }
+                }
+                __syncwarp();  // this buffer is refilled two steps on
             }
+            cp_async_wait0();
             release_last();
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {

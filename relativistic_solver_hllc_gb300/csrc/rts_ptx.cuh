@@ -167,6 +167,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 16-byte asynchronous global -> shared copy (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void prefetch_l2(const void* p)
 {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -245,6 +254,37 @@ __device__ __forceinline__ float join_any(bool fp16, uint16_t hi, uint16_t lo)
 }
 
 __host__ __device__ __forceinline__ uint32_t pack2(uint16_t a, uint16_t b) { return (uint32_t)a | ((uint32_t)b << 16); }
+
+// Two values at once (first in the low half), bit-identical to split_any /
+// join_any on each value.
+__device__ __forceinline__ void split2_any(bool fp16, float x0, float x1, uint32_t& hi2, uint32_t& lo2)
+{
+    if (fp16) {
+        const __half2 h = __floats2half2_rn(x0, x1);
+        const float2 b = __half22float2(h);
+        const __half2 l = __floats2half2_rn(x0 - b.x, x1 - b.y);
+        hi2 = *reinterpret_cast<const uint32_t*>(&h);
+        lo2 = *reinterpret_cast<const uint32_t*>(&l);
+    } else {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        const float2 b = __bfloat1622float2(h);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - b.x, x1 - b.y);
+        hi2 = *reinterpret_cast<const uint32_t*>(&h);
+        lo2 = *reinterpret_cast<const uint32_t*>(&l);
+    }
+}
+__device__ __forceinline__ float2 join2_any(bool fp16, uint32_t hi2, uint32_t lo2)
+{
+    float2 h, l;
+    if (fp16) {
+        h = __half22float2(*reinterpret_cast<const __half2*>(&hi2));
+        l = __half22float2(*reinterpret_cast<const __half2*>(&lo2));
+    } else {
+        h = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hi2));
+        l = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&lo2));
+    }
+    return make_float2(h.x + l.x, h.y + l.y);
+}
 
 // offset (in halves) of the high part of in-direction j inside an interleaved
 // split row: per 32 in-directions, 32 high halves then 32 low halves
