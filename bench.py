@@ -61,8 +61,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
-    ap.add_argument("--flush", type=int, default=0, choices=[0, 1, 2],
-                    help="tensor-core K-slices per FP32 drain (0: library default, 1)")
+    ap.add_argument("--flush", type=int, default=2, choices=[0, 1, 2],
+                    help="tensor-core K-slices per FP32 drain (library default 1; 2 halves the drains and "
+                         "still meets the 1e-6 gate on this workload, checked in the same run)")
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
                     help="2: the headline source iteration (default); 1, 3, 4, 5: the other configurations")
     return ap.parse_args()
@@ -425,6 +426,7 @@ def run_ours(args, rank, world, local):
         "dtype": dtype, "data": "synthetic",
         "config": {"workload": WORKLOAD["name"], "cells": N, "dirs": M, "precision": prec,
                    "flush": args.flush or 1,
+                   "accuracy_gate": "max rel err vs FP64 path <= 1e-6 after the timed steps (see accuracy)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (no flush)", "step": "integral + update + residual + relaxation"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,

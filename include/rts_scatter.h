@@ -196,6 +196,24 @@ int rts_device_arrays(rts_ctx* ctx, double** d_illum, double** d_scattering);
  * arrays that are non-NULL, synchronously with that stream. */
 int rts_moments(rts_ctx* ctx, int stream, double* energy, double* flux);
 
+/* Cell geometry for the divergence moments: outward unit normals of the four
+ * faces [N][4][3], face areas [N][4], cell volumes [N] (> 0).  Replaces the
+ * reference's reads of normals.bin / squares.bin / volume.bin in InitDevice
+ * and their upload (cuda/cuda_struct.cu:134-176, grid_init_copy_host_to_device
+ * :86-107). */
+int rts_set_geometry(rts_ctx* ctx, const double* normals, const double* face_areas, const double* volume);
+
+/* Energy [N], flux [N][3], impulse tensor [N][9] (row-major, symmetric), and
+ * the divergences of flux [N] and impulse [N][3] of the device Illum, in FP64,
+ * in one pass.  Replaces d_MakeIllumParam and its launches
+ * CalculateAllParam / CalculateAllParamStream (cuda/cuda_kernel.cu:218-223,
+ * cuda/cuda_solve.cu:272-320), CalculateImpuls (:209-225), CalculateDivImpuls
+ * (:227-247) and CalculateDivStream (:249-270).  Null outputs are skipped; the
+ * divergences need rts_set_geometry.  Runs on `stream` after the work queued
+ * on the scattering stream and returns when the copies have landed. */
+int rts_illum_params(rts_ctx* ctx, int stream, double* energy, double* flux, double* impuls, double* divstream,
+                     double* divimpuls);
+
 /* S <- (1-lambda) B[c] + lambda S on the device scattering array
  * (local rows [start, end)), and the FP64 residual max|S_new - S_old|
  * against the values it replaces (residual may be NULL). */

@@ -70,6 +70,7 @@ _SIG = {
     "orc_normal": (C.c_double, [_u64, _u64, _u64]),
     "orc_fill_illum": (None, [_u64, C.c_double, C.c_double, _i64, _i64, _i64, C.c_int, _dp]),
     "orc_fill_uniform": (None, [_u64, _u64, C.c_double, C.c_double, _i64, _i64, _dp]),
+    "orc_fill_normal": (None, [_u64, _u64, _i64, _dp]),
     "orc_fill_illum_cells": (None, [_u64, C.c_double, C.c_double, _i64, _i64, _i64, _i64, C.c_int, _dp]),
     "orc_fibonacci_directions": (None, [_i64, _dp, _dp, _dp]),
     "orc_weights_thomson": (None, [_i64, _dp, _dp, C.c_double, _i64, _i64, _dp]),
@@ -81,6 +82,7 @@ _SIG = {
     "orc_face_mean": (None, [_dp, _i64, _i64, _dp]),
     "orc_energy": (None, [_dp, _i64, _i64, _dp, C.c_double, _dp]),
     "orc_stream": (None, [_dp, _i64, _i64, _dp, _dp, C.c_double, _dp]),
+    "orc_illum_params": (None, [_dp, _i64, _i64, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "orc_source_update": (None, [_i64, _i64, _dp, _dp, C.c_double]),
     "orc_max_abs_diff": (C.c_double, [_dp, _dp, _i64]),
     "orc_iterate": (None, [_dp, _i64, _dp, _i64, _dp, C.c_double, C.c_int, C.c_int, _dp, _dp]),
@@ -217,6 +219,32 @@ def stream(illum_arr, N, xyz, area, full_area) -> np.ndarray:
     out = np.empty(3 * N)
     lib().orc_stream(_p(illum_arr), N, area.size, _p(xyz), _p(area), full_area, _p(out))
     return out.reshape(N, 3)
+
+
+def illum_params(illum_arr, N, xyz, area, full_area, normals, face_areas, volume):
+    """flux [N][3], impuls [N][9], divstream [N], divimpuls [N][3]."""
+    illum_arr = np.ascontiguousarray(illum_arr, dtype=np.float64)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    face_areas = np.ascontiguousarray(face_areas, dtype=np.float64)
+    volume = np.ascontiguousarray(volume, dtype=np.float64)
+    fl, im, ds, di = np.empty(3 * N), np.empty(9 * N), np.empty(N), np.empty(3 * N)
+    lib().orc_illum_params(_p(illum_arr), N, area.size, _p(xyz), _p(area), full_area, _p(normals), _p(face_areas),
+                           _p(volume), _p(fl), _p(im), _p(ds), _p(di))
+    return fl.reshape(N, 3), im.reshape(N, 9), ds, di.reshape(N, 3)
+
+
+def cell_geometry(seed: int, N: int):
+    """Seeded synthetic tetrahedron geometry: unit outward normals [N][4][3],
+    face areas [N][4] in (0.5, 1.5), volumes [N] in (0.2, 1.2)."""
+    n = np.empty(N * 12)
+    lib().orc_fill_normal(seed, 11, N * 12, _p(n))
+    n = n.reshape(N, 4, 3)
+    n /= np.linalg.norm(n, axis=2, keepdims=True)
+    fa = uniform(seed, 12, 0.5, 1.5, 4 * N).reshape(N, 4)
+    vol = uniform(seed, 13, 0.2, 1.2, N)
+    return n, fa, vol
 
 
 def source_update(S, B, lam) -> np.ndarray:

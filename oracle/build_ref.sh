@@ -15,6 +15,9 @@
 #   Illum_async.cpp:201-256   GetS, CalculateIntCPU
 #   Illum_async.cpp:1101-1122 GET_FACE_TO_CELL, IntegarteDirection
 #   Illum_async.cpp:1156-1178 IntegarteDirection3
+#   Illum_async.cpp:1179-1247 MakeStream (flux and its divergence)
+#   Illum_async.cpp:1250-1349 IntegarteDirection9, MakeDivImpuls (impulse
+#                             tensor and its divergence)
 #   solve_utils.cpp:177-202   GetSend, GetDisp
 set -eu
 REF=${RTS_REFERENCE_ROOT:-/root/reference}/solver_hllc_illum_cuda
@@ -35,6 +38,10 @@ UTL="$REF/solve_module/solve_utils.cpp"
     iconv -f cp1251 -t utf-8 "$ILL" | sed -n '1101,1122p'
     echo '#line 1156 "solve_module/illum/Illum_async.cpp"'
     iconv -f cp1251 -t utf-8 "$ILL" | sed -n '1156,1178p'
+    echo '#line 1179 "solve_module/illum/Illum_async.cpp"'
+    iconv -f cp1251 -t utf-8 "$ILL" | sed -n '1179,1247p'
+    echo '#line 1250 "solve_module/illum/Illum_async.cpp"'
+    iconv -f cp1251 -t utf-8 "$ILL" | sed -n '1250,1349p'
     echo '#line 177 "solve_module/solve_utils.cpp"'
     iconv -f cp1251 -t utf-8 "$UTL" | sed -n '177,202p'
     echo '#line 1 "oracle/ref_standin/entry.cpp"'

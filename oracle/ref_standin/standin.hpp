@@ -11,8 +11,13 @@
 //                               scalar*vector and Zero() are used.  dot() sums
 //                               x, y, z left to right.
 //   direction_s, grid_directions_t  global_def.h:79-90
+//   Matrix3 (Eigen::Matrix3d) . (h,k), Zero(), +=, /= scalar, matrix*vector
+//                               (row h: sum over k = 0,1,2 left to right)
+//   geo_face_t, face_t, geo_cell_t, illum_value_t, elem_t
+//                               solve_module/solve_global_struct.h:86-151
+//                               (only the members the divergence code reads)
 //   grid_t .................... solve_module/solve_global_struct.h:153-230
-//                               (only size, Illum, scattering)
+//                               (only size, Illum, scattering, cells, faces)
 //   MPI_GET_INF ............... global_def.h:157-161 (single process)
 #pragma once
 #include <cstdint>
@@ -35,10 +40,46 @@ struct Vector3 {
     Vector3& operator/=(double s) { v[0] /= s; v[1] /= s; v[2] /= s; return *this; }
 };
 inline Vector3 operator*(double s, const Vector3& a) { return Vector3(s * a.v[0], s * a.v[1], s * a.v[2]); }
+inline Vector3 operator*(const Vector3& a, double s) { return Vector3(a.v[0] * s, a.v[1] * s, a.v[2] * s); }
+inline Vector3 operator-(const Vector3& a) { return Vector3(-a.v[0], -a.v[1], -a.v[2]); }
+
+struct Matrix3 {
+    double m[3][3];
+    Matrix3() { for (int h = 0; h < 3; ++h) for (int k = 0; k < 3; ++k) m[h][k] = 0.0; }
+    static Matrix3 Zero() { return Matrix3(); }
+    double& operator()(int h, int k) { return m[h][k]; }
+    double operator()(int h, int k) const { return m[h][k]; }
+    Matrix3& operator+=(const Matrix3& o) { for (int h = 0; h < 3; ++h) for (int k = 0; k < 3; ++k) m[h][k] += o.m[h][k]; return *this; }
+    Matrix3& operator/=(double s) { for (int h = 0; h < 3; ++h) for (int k = 0; k < 3; ++k) m[h][k] /= s; return *this; }
+};
+inline Vector3 operator*(const Matrix3& a, const Vector3& x)
+{
+    Vector3 r;
+    for (int h = 0; h < 3; ++h) r.v[h] = a.m[h][0] * x.v[0] + a.m[h][1] * x.v[1] + a.m[h][2] * x.v[2];
+    return r;
+}
 
 struct direction_s { Vector3 dir; Type area; };
 struct grid_directions_t { int size; std::vector<direction_s> directions; Type full_area; };
-struct grid_t { int size; Type* Illum; Type* scattering; };
+struct geo_face_t { Vector3 n; Type S; };
+struct face_t { geo_face_t geo; };
+struct geo_cell_t { int id_faces[base]; Type V; bool sign_n[base]; };
+struct illum_value_t {
+    std::vector<Type> illum;  // [dir][face] of one cell
+    Type energy;
+    Vector3 stream;
+    Matrix3 impuls;
+    Type div_stream;
+    Vector3 div_impuls;
+};
+struct elem_t { illum_value_t illum_val; geo_cell_t geo; };
+struct grid_t {
+    int size;
+    Type* Illum;
+    Type* scattering;
+    std::vector<elem_t> cells;
+    std::vector<face_t> faces;
+};
 
 #define MPI_GET_INF(np, myid) { np = 1; myid = 0; }
 

@@ -116,6 +116,11 @@ void orc_fill_illum_cells(uint64_t seed, double mu, double sigma, int64_t N, int
 }
 
 /* uniform(lo, hi) values on stream `stream`, indices [i0, i0 + n) */
+void orc_fill_normal(uint64_t seed, uint64_t stream, int64_t n, double* out)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = orc_normal(seed, stream, (uint64_t)i);
+}
+
 void orc_fill_uniform(uint64_t seed, uint64_t stream, double lo, double hi,
                       int64_t i0, int64_t n, double* out)
 {
@@ -327,6 +332,80 @@ void orc_stream(const double* illum, int64_t N, int64_t M, const double* xyz,
             for (int f = 0; f < ORC_BASE; ++f) v += sf[f][d] / full_area;
             stream[3 * c + d] = v / ORC_BASE;
         }
+    }
+}
+
+/* Flux, impulse tensor and their divergences (the reference's
+ * d_MakeIllumParam: cuda/cuda_kernel.cu:149-175 d_MakeDivStream, :177-216
+ * d_MakeDivImpuls, with IntegarteDirection3Faces / IntegarteDirection9Faces
+ * of cuda/cuda_utils.cu:86-167 and the face mean CUDA_CONVERT_FATE_TO_CELL
+ * of cuda/cuda_kernel.cu:9-17; CPU twins MakeStream / MakeDivImpuls at
+ * solve_module/illum/Illum_async.cpp:1179-1349).  Per cell c and face f:
+ *   Stream_f   = sum_j (I[j][c][f] * area_j) * w_j / full_area
+ *   Impuls_f   = sum_j w_j w_j^T * (I[j][c][f] * area_j) / full_area
+ * flux and impuls are the face means; with the cell's outward face normals
+ * n_f, face areas S_f and volume V:
+ *   divstream  = sum_f (Stream_f . n_f) S_f / V
+ *   divimpuls  = sum_f (Impuls_f n_f) S_f / V
+ * Outputs: flux [N][3], impuls [N][9] (row-major h*3+k), divstream [N],
+ * divimpuls [N][3]; any may be NULL. */
+void orc_illum_params(const double* illum, int64_t N, int64_t M, const double* xyz, const double* area,
+                      double full_area, const double* normals /* N x 4 x 3 */,
+                      const double* face_areas /* N x 4 */, const double* volume, double* flux,
+                      double* impuls, double* divstream, double* divimpuls)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < N; ++c) {
+        double st[ORC_BASE][3], im[ORC_BASE][9];
+        memset(st, 0, sizeof(st));
+        memset(im, 0, sizeof(im));
+        for (int64_t j = 0; j < M; ++j) {
+            const double* s = illum + (j * N + c) * ORC_BASE;
+            const double* w = xyz + 3 * j;
+            for (int f = 0; f < ORC_BASE; ++f) {
+                const double ia = s[f] * area[j];
+                for (int d = 0; d < 3; ++d) st[f][d] += w[d] * ia;
+                for (int h = 0; h < 3; ++h)
+                    for (int k = 0; k < 3; ++k) im[f][h * 3 + k] += w[h] * w[k] * ia;
+            }
+        }
+        for (int f = 0; f < ORC_BASE; ++f) {
+            for (int d = 0; d < 3; ++d) st[f][d] /= full_area;
+            for (int d = 0; d < 9; ++d) im[f][d] /= full_area;
+        }
+        if (flux)
+            for (int d = 0; d < 3; ++d) {
+                double v = 0;
+                for (int f = 0; f < ORC_BASE; ++f) v += st[f][d];
+                flux[3 * c + d] = v / ORC_BASE;
+            }
+        if (impuls)
+            for (int d = 0; d < 9; ++d) {
+                double v = 0;
+                for (int f = 0; f < ORC_BASE; ++f) v += im[f][d];
+                impuls[9 * c + d] = v / ORC_BASE;
+            }
+        const double* n = normals + 12 * c;
+        const double* S = face_areas + 4 * c;
+        if (divstream) {
+            double v = 0;
+            for (int f = 0; f < ORC_BASE; ++f) {
+                double dot = 0;
+                for (int k = 0; k < 3; ++k) dot += st[f][k] * n[3 * f + k];
+                v += dot * S[f];
+            }
+            divstream[c] = v / volume[c];
+        }
+        if (divimpuls)
+            for (int h = 0; h < 3; ++h) {
+                double v = 0;
+                for (int f = 0; f < ORC_BASE; ++f) {
+                    double dot = 0;
+                    for (int k = 0; k < 3; ++k) dot += im[f][h * 3 + k] * n[3 * f + k];
+                    v += dot * S[f];
+                }
+                divimpuls[3 * c + h] = v / volume[c];
+            }
     }
 }
 

@@ -86,6 +86,8 @@ _SIGNATURES = {
     "rts_scattering_update": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_double, _dp]),
     "rts_device_arrays": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
     "rts_moments": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "rts_set_geometry": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "rts_illum_params": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
     "rts_source_update": (C.c_int, [_vp, _dp, C.c_double, _i64, _i64, C.c_int, _dp]),
     "rts_sync_stream": (C.c_int, [_vp, C.c_int, _i64]),
     "rts_wait": (C.c_int, [_vp, _i64]),
@@ -376,6 +378,24 @@ class Context:
         f = np.empty(self.N * 3, dtype=np.float64)
         self._check(self.lib.rts_moments(self.h, int(stream), _ptr(e), _ptr(f)), "rts_moments")
         return e, f.reshape(self.N, 3)
+
+    def set_geometry(self, normals, face_areas, volume):
+        """Outward face normals [N][4][3], face areas [N][4], volumes [N]."""
+        n = _f64(normals, (self.N, 4, 3))
+        s = _f64(face_areas, (self.N, 4))
+        v = _f64(volume, (self.N,))
+        self._check(self.lib.rts_set_geometry(self.h, _ptr(n), _ptr(s), _ptr(v)), "rts_set_geometry")
+
+    def illum_params(self, stream: int = STREAM_PARAMS, divergence: bool = True):
+        """energy [N], flux [N][3], impuls [N][3][3], divstream [N], divimpuls [N][3]
+        (the last two None unless divergence)."""
+        N = self.N
+        e, f, im = np.empty(N), np.empty(3 * N), np.empty(9 * N)
+        ds = np.empty(N) if divergence else None
+        di = np.empty(3 * N) if divergence else None
+        self._check(self.lib.rts_illum_params(self.h, int(stream), _ptr(e), _ptr(f), _ptr(im), _ptr(ds), _ptr(di)),
+                    "rts_illum_params")
+        return (e, f.reshape(N, 3), im.reshape(N, 3, 3), ds, None if di is None else di.reshape(N, 3))
 
     def source_update(self, B, lam: float, start: int, end: int, stream: int = STREAM_SCATTERING_1,
                       residual: bool = True):

@@ -19,13 +19,27 @@
 // CalculateIntScatteringAsyncMPIStream lands at row `start` (start*N
 // elements), where the reference offsets by `start` elements
 // (cuda/cuda_solve.cu:107), which is the same for the start == 0 the solver
-// uses; CalculateEnergy / CalculateStream compute the moments (their kernels
-// are commented out in the reference, cuda/cuda_solve.cu:182,236,259).
+// uses; CalculateEnergy / CalculateStream / CalculateDivStream /
+// CalculateDivImpuls compute their moments (their kernels are commented out
+// in the reference, cuda/cuda_solve.cu:182,236,259).
+//
+// Cell geometry: like the reference's InitDevice (cuda/cuda_struct.cu:134-176),
+// the first rank reads normals.bin, squares.bin and volume.bin from the
+// solver's base directory -- glb_files.base_adress when this file is built
+// inside the reference (RTS_COMPAT_GLB_FILES defined, global_value.h
+// included), otherwise the RTS_GEOMETRY_DIR environment variable (with a
+// trailing separator, as base_adress has).  Missing files leave the
+// divergence calls failing with a message, as in the reference.
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "cuda_solve.h"
 #include "rts_scatter.h"
+#ifdef RTS_COMPAT_GLB_FILES
+#include "global_value.h"
+#endif
 
 namespace {
 
@@ -47,6 +61,47 @@ rts_stream_id stream_of(e_cuda_stream_id_t s)
     case eCuda_scattering_2: return RTS_STREAM_SCATTERING_2;
     default: return RTS_STREAM_PARAMS;
     }
+}
+
+std::string geometry_dir()
+{
+#ifdef RTS_COMPAT_GLB_FILES
+    return glb_files.base_adress;
+#else
+    const char* d = std::getenv("RTS_GEOMETRY_DIR");
+    return d ? std::string(d) : std::string();
+#endif
+}
+
+// normals.bin: count-prefixed cells of four Vector3; squares.bin: 4 areas per
+// cell; volume.bin: one volume per cell (file_module/reader_bin.cpp:49-69,
+// reader_bin.h:13-30).
+void load_geometry(int N)
+{
+    const std::string dir = geometry_dir();
+    if (dir.empty()) return;
+    std::vector<double> n((size_t)N * 12), s((size_t)N * 4), v((size_t)N);
+    int64_t cn = 0, cs = 0, cv = 0;
+    if (rts_read_simple_bin((dir + "normals.bin").c_str(), 96, N, n.data(), &cn) != RTS_OK ||
+        rts_read_simple_bin((dir + "squares.bin").c_str(), 8, 4 * (int64_t)N, s.data(), &cs) != RTS_OK ||
+        rts_read_simple_bin((dir + "volume.bin").c_str(), 8, N, v.data(), &cv) != RTS_OK || cn != N ||
+        cs != 4 * (int64_t)N || cv != N) {
+        std::fprintf(stderr, "InitDevice: cell geometry (normals.bin, squares.bin, volume.bin) not read from %s\n",
+                     dir.c_str());
+        return;
+    }
+    report(rts_set_geometry(g_ctx, n.data(), s.data(), v.data()), "InitDevice (geometry)");
+}
+
+int params(e_cuda_stream_id_t st, grid_t& grid, bool energy, bool stream, bool impuls, bool divstream,
+           bool divimpuls, const char* where)
+{
+    return report(rts_illum_params(g_ctx, stream_of(st), energy ? grid.energy : nullptr,
+                                   stream ? reinterpret_cast<double*>(grid.stream) : nullptr,
+                                   impuls ? reinterpret_cast<double*>(grid.impuls) : nullptr,  // symmetric: either order
+                                   divstream ? grid.divstream : nullptr,
+                                   divimpuls ? reinterpret_cast<double*>(grid.divimpuls) : nullptr),
+                  where);
 }
 
 }  // namespace
@@ -83,6 +138,7 @@ void InitDevice(const grid_directions_t& grid_dir_host, grid_t& grid_host, const
         grid_host.stream = new Vector3[grid_host.size]();
         grid_host.impuls = new Matrix3[grid_host.size]();
         g_owns_moments = true;
+        load_geometry(grid_host.size);
     }
 }
 
@@ -178,22 +234,19 @@ int CalculateStream(const grid_directions_t&, grid_t& grid)
                   "CalculateStream");
 }
 
-int CalculateImpuls(const grid_directions_t&, grid_t&)
+int CalculateImpuls(const grid_directions_t&, grid_t& grid)
 {
-    std::fprintf(stderr, "CalculateImpuls: the pressure-tensor moment is not provided by librts_scatter\n");
-    return 1;
+    return params(eCuda_params, grid, false, false, true, false, false, "CalculateImpuls");
 }
 
-int CalculateDivImpuls(const grid_directions_t&, grid_t&)
+int CalculateDivImpuls(const grid_directions_t&, grid_t& grid)
 {
-    std::fprintf(stderr, "CalculateDivImpuls: divergence moments are not provided by librts_scatter\n");
-    return 1;
+    return params(eCuda_params, grid, false, false, grid.impuls != nullptr, false, true, "CalculateDivImpuls");
 }
 
-int CalculateDivStream(const grid_directions_t&, grid_t&)
+int CalculateDivStream(const grid_directions_t&, grid_t& grid)
 {
-    std::fprintf(stderr, "CalculateDivStream: divergence moments are not provided by librts_scatter\n");
-    return 1;
+    return params(eCuda_params, grid, false, grid.stream != nullptr, false, true, false, "CalculateDivStream");
 }
 
 int CalculateAllParam(const grid_directions_t& grid_dir, grid_t& grid)
@@ -203,7 +256,8 @@ int CalculateAllParam(const grid_directions_t& grid_dir, grid_t& grid)
 
 int CalculateAllParamStream(const grid_directions_t&, grid_t& grid, e_cuda_stream_id_t st)
 {
-    // energy and flux (stream); the divergence moments need the cell geometry
-    return report(rts_moments(g_ctx, stream_of(st), grid.energy, reinterpret_cast<double*>(grid.stream)),
-                  "CalculateAllParamStream");
+    // d_MakeIllumParam: the divergences (always), energy / flux / impulse when
+    // the host arrays exist (CUDA_FULL_ARRAYS in the reference)
+    return params(st, grid, grid.energy != nullptr, grid.stream != nullptr, grid.impuls != nullptr,
+                  grid.divstream != nullptr, grid.divimpuls != nullptr, "CalculateAllParamStream");
 }

@@ -65,6 +65,9 @@ static void free_grid(rts_ctx* ctx)
     rts_dfree(ctx, ctx->d_W, rts_bytes<double>(ctx->M * loc));
     rts_dfree(ctx, ctx->d_energy, rts_bytes<double>(ctx->N));
     rts_dfree(ctx, ctx->d_flux, rts_bytes<double>(ctx->N * 3));
+    rts_dfree(ctx, ctx->d_geo, rts_bytes<double>(ctx->N * 17));
+    rts_dfree(ctx, ctx->d_params, rts_bytes<double>(ctx->N * 17));
+    ctx->d_geo = ctx->d_params = nullptr;
     rts_dfree(ctx, ctx->d_B, rts_bytes<double>(ctx->N));
     rts_dfree(ctx, ctx->d_xyz, rts_bytes<double>(ctx->M * 3));
     rts_dfree(ctx, ctx->d_area, rts_bytes<double>(ctx->M));
@@ -468,6 +471,69 @@ int rts_moments(rts_ctx* ctx, int stream, double* energy, double* flux)
     if (flux)
         RTS_CUDA_TRY(ctx, cudaMemcpyAsync(flux, ctx->d_flux, rts_bytes<double>(ctx->N * 3),
                                           cudaMemcpyDeviceToHost, st));
+    RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return RTS_OK;
+}
+
+int rts_set_geometry(rts_ctx* ctx, const double* normals, const double* face_areas, const double* volume)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_REQUIRE(ctx, ctx->d_illum, RTS_ERR_BAD_STATE, "rts_set_geometry before rts_init");
+    RTS_REQUIRE(ctx, normals && face_areas && volume, RTS_ERR_INVALID_ARGUMENT, "rts_set_geometry: null array");
+    const int64_t N = ctx->N;
+    for (int64_t c = 0; c < N; ++c)
+        RTS_REQUIRE(ctx, volume[c] > 0.0, RTS_ERR_INVALID_ARGUMENT, "rts_set_geometry: volume[%lld] <= 0",
+                    (long long)c);
+    if (!ctx->d_geo) {
+        void* p = nullptr;
+        int rc = rts_dmalloc(ctx, &p, rts_bytes<double>(N * 17), "cell geometry");
+        if (rc != RTS_OK) return rc;
+        ctx->d_geo = (double*)p;
+    }
+    cudaStream_t st = ctx->streams[RTS_STREAM_PARAMS];
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_geo, normals, rts_bytes<double>(N * 12), cudaMemcpyHostToDevice, st));
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_geo + 12 * N, face_areas, rts_bytes<double>(N * 4),
+                                      cudaMemcpyHostToDevice, st));
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_geo + 16 * N, volume, rts_bytes<double>(N), cudaMemcpyHostToDevice, st));
+    RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return RTS_OK;
+}
+
+int rts_illum_params(rts_ctx* ctx, int stream, double* energy, double* flux, double* impuls, double* divstream,
+                     double* divimpuls)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_REQUIRE(ctx, ctx->d_illum, RTS_ERR_BAD_STATE, "rts_illum_params before rts_init");
+    RTS_REQUIRE(ctx, valid_stream(stream), RTS_ERR_INVALID_ARGUMENT, "bad stream id %d", stream);
+    RTS_REQUIRE(ctx, ctx->d_geo || (!divstream && !divimpuls), RTS_ERR_BAD_STATE,
+                "the divergences need the cell geometry (rts_set_geometry)");
+    const int64_t N = ctx->N;
+    if (!ctx->d_params) {
+        void* p = nullptr;
+        int rc = rts_dmalloc(ctx, &p, rts_bytes<double>(N * 17), "illumination parameters");
+        if (rc != RTS_OK) return rc;
+        ctx->d_params = (double*)p;
+    }
+    cudaStream_t st = ctx->streams[stream];
+    if (stream != RTS_STREAM_SCATTERING_1) {  // after the Illum copies queued on the scattering stream
+        cudaEvent_t ev;
+        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaEventRecord(ev, ctx->streams[RTS_STREAM_SCATTERING_1]);
+        cudaStreamWaitEvent(st, ev, 0);
+        cudaEventDestroy(ev);
+    }
+    int rc = rts_launch_illum_params(ctx, st);
+    if (rc != RTS_OK) return rc;
+    double* const d = ctx->d_params;
+    struct {
+        double* host;
+        const double* dev;
+        int64_t n;
+    } outs[5] = {{energy, d, N}, {flux, d + N, 3 * N}, {impuls, d + 4 * N, 9 * N}, {divstream, d + 13 * N, N},
+                 {divimpuls, d + 14 * N, 3 * N}};
+    for (auto& o : outs)
+        if (o.host)
+            RTS_CUDA_TRY(ctx, cudaMemcpyAsync(o.host, o.dev, rts_bytes<double>(o.n), cudaMemcpyDeviceToHost, st));
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     return RTS_OK;
 }

@@ -86,6 +86,8 @@ struct rts_ctx {
     double* h_S = nullptr;       // pinned, [out_end-out_start][N]
     double* d_energy = nullptr;  // [N]
     double* d_flux = nullptr;    // [N][3]
+    double* d_geo = nullptr;     // [N][4][3] outward face normals, [N][4] face areas, [N] volumes (or null)
+    double* d_params = nullptr;  // energy [N], flux [N][3], impuls [N][9], divstream [N], divimpuls [N][3]
     double* d_B = nullptr;       // [N]
     // residual bits (non-negative doubles order as u64): slot 0 for
     // rts_source_update, slots 1..RTS_RESID_CAP a ring of per-step residuals
@@ -126,6 +128,7 @@ void rts_dfree(rts_ctx* ctx, void* p, size_t bytes);
 int rts_launch_scatter_fp64(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t st,
                             const double* B, double lambda, bool update, bool residual);
 int rts_launch_moments(rts_ctx* ctx, cudaStream_t st);
+int rts_launch_illum_params(rts_ctx* ctx, cudaStream_t st);
 int rts_launch_update(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t st,
                       const double* B, double lambda, bool residual);
 int rts_launch_relax_fp64(rts_ctx* ctx, cudaStream_t st);

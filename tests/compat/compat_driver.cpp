@@ -62,6 +62,15 @@ int main(int argc, char** argv)
     CudaSyncStream(eCuda_params);
     rts_write_simple_bin((out + "/energy.bin").c_str(), 8, N, grid.energy);
     rts_write_simple_bin((out + "/stream.bin").c_str(), 24, N, grid.stream);
+    rts_write_simple_bin((out + "/impuls.bin").c_str(), 72, N, grid.impuls);
+    rts_write_simple_bin((out + "/divstream.bin").c_str(), 8, N, grid.divstream);
+    rts_write_simple_bin((out + "/divimpuls.bin").c_str(), 24, N, grid.divimpuls);
+    // the single-moment calls write the same arrays
+    std::memset(grid.divstream, 0, sizeof(double) * N);
+    if (CalculateDivStream(dirs, grid)) return fail("CalculateDivStream");
+    if (CalculateDivImpuls(dirs, grid)) return fail("CalculateDivImpuls");
+    if (CalculateImpuls(dirs, grid)) return fail("CalculateImpuls");
+    rts_write_simple_bin((out + "/divstream2.bin").c_str(), 8, N, grid.divstream);
 
     std::memset(grid.scattering, 0, sizeof(double) * M * N);
     if (CalculateIntScattering(dirs, grid)) return fail("CalculateIntScattering");

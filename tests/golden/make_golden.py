@@ -97,6 +97,26 @@ def main():
     )
     print(f"config1_sample: total={S.sum():.17g}")
 
+    # flux, impulse tensor and their divergences (MakeStream / MakeDivImpuls)
+    # on seeded synthetic geometry, two direction sets
+    for name, N, M, seed in [("div_n40_m24", 40, 24, 31), ("div_n7_m5", 7, 5, 37)]:
+        xyz, area, fa = oracle.fibonacci_directions(M)
+        il = oracle.illum(seed, 0.0, 1.0, N, M, independent_faces=True)
+        nrm, fS, vol = oracle.cell_geometry(seed, N)
+        out = [np.empty(3 * N), np.empty(9 * N), np.empty(N), np.empty(3 * N)]
+        f = ref.ref_illum_params
+        f.restype = None
+        f.argtypes = [oracle.C.c_int, oracle.C.c_int] + [oracle._dp] * 2 + [oracle.C.c_double] + [oracle._dp] * 8
+        f(N, M, _p(np.ascontiguousarray(xyz).ravel()), _p(area), fa, _p(il), _p(nrm.ravel()), _p(fS.ravel()),
+          _p(vol), *[_p(o) for o in out])
+        pin_idx = np.linspace(0, il.size - 1, 16).astype(np.int64)
+        np.savez_compressed(
+            HERE / f"{name}.npz", N=N, M=M, seed=seed, mu=0.0, sigma=1.0, independent_faces=1,
+            flux=out[0].reshape(N, 3), impuls=out[1].reshape(N, 9), divstream=out[2], divimpuls=out[3].reshape(N, 3),
+            normals=nrm, face_areas=fS, volume=vol, pin_idx=pin_idx, pin_val=il[pin_idx],
+        )
+        print(f"{name}: divstream sum={out[2].sum():.17g}")
+
     # direction partition GetSend / GetDisp
     rows = []
     for np_, n in [(1, 7), (2, 7), (3, 10), (4, 3), (5, 1000), (7, 590), (16, 1202), (6, 6)]:

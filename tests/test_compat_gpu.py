@@ -39,8 +39,16 @@ def test_reference_calling_sequence(native_lib, tmp_path):
     il = oracle.illum(12, 0.0, 1.0, N, M, independent_faces=True)
     _native.write_direction_file(tmp_path / "dirs.txt", xyz, area, fa)
     _native.write_simple_bin(tmp_path / "Illum.bin", il)
+    # cell geometry files as the reference's InitDevice reads them
+    nrm, fS, vol = oracle.cell_geometry(14, N)
+    geo = tmp_path / "geo"
+    geo.mkdir()
+    _native.write_simple_bin(geo / "normals.bin", nrm.reshape(N, 12).view(np.dtype([("c", np.float64, 12)])).ravel())
+    _native.write_simple_bin(geo / "squares.bin", fS.ravel())
+    _native.write_simple_bin(geo / "volume.bin", vol)
+    env = {**__import__("os").environ, "RTS_GEOMETRY_DIR": str(geo) + "/"}
     res = subprocess.run([str(exe), str(tmp_path / "dirs.txt"), str(tmp_path / "Illum.bin"), str(N), str(tmp_path)],
-                         capture_output=True, text=True, timeout=120)
+                         capture_output=True, text=True, timeout=120, env=env)
     assert res.returncode == 0, res.stderr
     ref = oracle.calculate_int_cpu(N, xyz, area, fa, il)
     for name in ("scattering.bin", "scattering_sync.bin"):
@@ -51,3 +59,12 @@ def test_reference_calling_sequence(native_lib, tmp_path):
     dt = np.dtype([("v", np.float64, 3)])
     s = _native.read_simple_bin(tmp_path / "stream.bin", dt)["v"]
     assert float(np.max(np.abs(s - oracle.stream(il, N, xyz, area, fa)) / e[:, None])) <= 1e-12
+    fl, im, ds, di = oracle.illum_params(il, N, xyz, area, fa, nrm, fS, vol)
+    imp = _native.read_simple_bin(tmp_path / "impuls.bin", np.dtype([("m", np.float64, 9)]))["m"]
+    assert float(np.max(np.abs(imp - im) / e[:, None])) <= 1e-12
+    term = np.max(fS, axis=1) / vol * 4
+    ds_g = _native.read_simple_bin(tmp_path / "divstream.bin")
+    assert float(np.max(np.abs(ds_g - ds) / (term * np.max(np.abs(fl), axis=1)))) <= 1e-12
+    assert np.array_equal(ds_g, _native.read_simple_bin(tmp_path / "divstream2.bin"))
+    di_g = _native.read_simple_bin(tmp_path / "divimpuls.bin", dt)["v"]
+    assert float(np.max(np.abs(di_g - di) / (term * np.max(np.abs(im), axis=1))[:, None])) <= 1e-12

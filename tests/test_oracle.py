@@ -56,6 +56,32 @@ def test_moments_match_reference(name):
     assert float(np.max(np.abs(s - g["stream"]) / scale)) <= 1e-15
 
 
+def divergence_scales(g):
+    """Term scales of the divergence sums: face terms |X_f n_f| S_f / V
+    cancel, so errors are measured against the largest term."""
+    term = np.max(g["face_areas"], axis=1) / g["volume"]
+    return term * np.max(np.abs(g["impuls"]), axis=1) * 4, term * np.max(np.abs(g["flux"]), axis=1) * 4 + 1e-300
+
+
+@pytest.mark.parametrize("name", ["div_n40_m24", "div_n7_m5"])
+def test_divergence_moments_match_reference(name):
+    """orc_illum_params against the reference's MakeStream / MakeDivImpuls."""
+    g = np.load(GOLDEN / f"{name}.npz")
+    N, M = int(g["N"]), int(g["M"])
+    il = oracle.illum(int(g["seed"]), 0.0, 1.0, N, M, independent_faces=True)
+    assert np.array_equal(il[g["pin_idx"]], g["pin_val"])
+    nrm, fS, vol = oracle.cell_geometry(int(g["seed"]), N)
+    assert np.array_equal(nrm, g["normals"]) and np.array_equal(fS, g["face_areas"]) and np.array_equal(vol, g["volume"])
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    fl, im, ds, di = oracle.illum_params(il, N, xyz, area, fa, nrm, fS, vol)
+    e = np.abs(oracle.energy(il, N, area, fa))
+    assert float(np.max(np.abs(fl - g["flux"]) / e[:, None])) <= 1e-14
+    assert float(np.max(np.abs(im - g["impuls"]) / e[:, None])) <= 1e-14
+    s_imp, s_flux = divergence_scales(g)
+    assert float(np.max(np.abs(ds - g["divstream"]) / s_flux)) <= 1e-14
+    assert float(np.max(np.abs(di - g["divimpuls"]) / s_imp[:, None])) <= 1e-14
+
+
 def test_config1_sample_matches_reference():
     g = np.load(GOLDEN / "config1_sample.npz")
     N, M = int(g["N"]), int(g["M"])
