@@ -192,8 +192,11 @@ def config5_requests(rate, duration, seed, max_requests=4000):
     return reqs
 
 
-def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2.0, precision="fp16x3"):
-    cap = 120 << 30
+def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2.0, precision="fp16x3",
+            policy=1, budget=0):
+    cap = 120 * 10**9
+    ctx.set_tuning(native.TUNE_SERVE_POLICY, policy)
+    ctx.set_tuning(native.TUNE_SERVE_BUDGET, budget)
     # host input pool (pinned), generated on the device
     pool_n = 500000 * 1202
     pool = native.PinnedBuffer(pool_n * 4 + 500000 * 4)
@@ -218,15 +221,29 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
     sat_specs = config5_requests(0.0, 0.0, seed=5, max_requests=96)
     st, _ = native.serve(ctx, build(sat_specs), cap)
     sat = st.throughput
-    mean_work = np.mean([N * M * it for (_, N, M, _, it) in sat_specs])
-    results = {"saturation_cell_dir_iter_per_s": sat, "saturation_requests": len(sat_specs), "loads": []}
+    # mean work of the request distribution, from a large sample of it (the
+    # heavy-tailed sizes make a small sample's mean unreliable)
+    pop = config5_requests(0.0, 0.0, seed=999, max_requests=4000)
+    mean_work = np.mean([N * M * it for (_, N, M, _, it) in pop])
+    results = {"saturation_cell_dir_iter_per_s": sat, "saturation_requests": len(sat_specs),
+               "policy": {0: "all resident", 1: "earliest deadline first within a tile budget",
+                          2: "least remaining work first within a tile budget"}[policy],
+               "tile_budget": budget or "8 waves",
+               "loads": []}
     for f in loads:
         rate = f * sat / mean_work
         specs = config5_requests(rate, window_s, seed=int(100 * f) + 7)
+        # rescale the Poisson arrival times so that the offered work is
+        # exactly f of the saturated throughput over the arrival span
+        work = sum(N * M * it for (_, N, M, _, it) in specs)
+        span = work / (f * sat)
+        t_last = specs[-1][0] if specs and specs[-1][0] > 0 else 1.0
+        specs = [(t * span / t_last, N, M, g, it) for (t, N, M, g, it) in specs]
+        offered = work / span / sat
         reqs = build(specs)
         st, lat = native.serve(ctx, reqs, cap)
         ok = lat[lat >= 0]
-        row = {"load": f, "rate_per_s": rate, "requests": len(reqs), "completed": st.completed,
+        row = {"load": f, "offered_load": offered, "rate_per_s": rate, "requests": len(reqs), "completed": st.completed,
                "rejected": st.rejected, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
                "throughput_cell_dir_iter_per_s": st.throughput, "max_active": st.max_active,
                "peak_gb": st.peak_bytes / 1e9}
@@ -245,6 +262,7 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
             row["p99_vs_isolated_p99"] = st.p99_ms / float(np.percentile(iso, 99))
         results["loads"].append(row)
     pool.close()
+    ctx.set_tuning(native.TUNE_SERVE_POLICY, 1)
     return results
 
 

@@ -422,6 +422,16 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
  *   default, -1 = no correction, n > 0 = a custom fraction of n * 1e-10. */
 #define RTS_TUNE_FLUSH 1
 #define RTS_TUNE_BIAS 2
+/*   RTS_TUNE_SERVE_POLICY: how rts_serve_run chooses the requests a step
+ *   advances: 1 (default) earliest deadline first, the deadline being arrival
+ *   + 2 x the request's estimated solve time alone; 2 least remaining work
+ *   first, a request left out gaining priority with every step it waits;
+ *   both within a tile budget; 0 every resident request every step.
+ *   RTS_TUNE_SERVE_BUDGET: tiles (128 cells x up to 256 directions) per step
+ *   under policies 1 and 2; 0 = 8 waves of the SMs.  At least one request
+ *   always runs. */
+#define RTS_TUNE_SERVE_POLICY 3
+#define RTS_TUNE_SERVE_BUDGET 4
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* The cudaStream_t of a stream slot (for callers that order their own work

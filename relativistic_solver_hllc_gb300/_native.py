@@ -60,6 +60,8 @@ class RtsError(RuntimeError):
 
 TUNE_FLUSH = 1  # RTS_TUNE_FLUSH
 TUNE_BIAS = 2   # RTS_TUNE_BIAS
+TUNE_SERVE_POLICY = 3  # RTS_TUNE_SERVE_POLICY
+TUNE_SERVE_BUDGET = 4  # RTS_TUNE_SERVE_BUDGET
 
 _dp = C.POINTER(C.c_double)
 _i64 = C.c_int64

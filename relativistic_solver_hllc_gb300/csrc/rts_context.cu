@@ -763,6 +763,14 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
                     "flush period %d outside [0, 2]", value);
         ctx->split_flush = value;
         return RTS_OK;
+    case RTS_TUNE_SERVE_POLICY:
+        RTS_REQUIRE(ctx, value >= 0 && value <= 2, RTS_ERR_INVALID_ARGUMENT, "serving policy %d not 0, 1 or 2", value);
+        ctx->serve_policy = value;
+        return RTS_OK;
+    case RTS_TUNE_SERVE_BUDGET:
+        RTS_REQUIRE(ctx, value >= 0, RTS_ERR_INVALID_ARGUMENT, "tile budget %d below 0", value);
+        ctx->serve_budget = value;
+        return RTS_OK;
     case RTS_TUNE_BIAS:
         RTS_REQUIRE(ctx, value >= -1, RTS_ERR_INVALID_ARGUMENT, "bias correction %d below -1", value);
         ctx->split_bias = value;

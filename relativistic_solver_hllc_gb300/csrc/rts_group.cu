@@ -85,6 +85,10 @@ struct rts_batch {
     int graph_steps = 0, graph_relax = 0;
     int64_t total_tiles = 0;
     int64_t steps = 0;
+    GroupProblem* h_pin[2] = {nullptr, nullptr};  // pinned staging of subset tables
+    size_t pin_cap = 0;
+    cudaEvent_t pin_ev[2] = {nullptr, nullptr};
+    int pin_next = 0;
 };
 
 namespace {
@@ -277,7 +281,80 @@ void rts_group_batch_free(rts_batch* b)
     rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
     rts_dfree(ctx, b->staging, b->staging_bytes);
     rts_dfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double));
+    for (int k = 0; k < 2; ++k) {
+        if (b->h_pin[k]) cudaFreeHost(b->h_pin[k]);
+        if (b->pin_ev[k]) cudaEventDestroy(b->pin_ev[k]);
+    }
     delete b;
+}
+
+static bool relaxes(const GProb* p, int relax)
+{
+    return p->S32 != nullptr && relax && p->a[1] && p->Mout == p->M;
+}
+
+// One problem's entry of the device table: entry `i`, its tiles starting at
+// `tiles` (advanced past them).
+static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& tiles, GroupProblem& g)
+{
+    rts_ctx* ctx = b->ctx;
+    memset(&g, 0, sizeof(g));
+    memcpy(&g.mapA[0], p->maps[0], 128);
+    memcpy(&g.mapA[1], p->maps[1], 128);
+    memcpy(&g.mapW, p->maps[2], 128);
+    g.N = p->N;
+    g.ldS = p->ldS > 0 ? p->ldS : p->N;
+    g.rows = p->rows;
+    g.tile_begin = tiles;
+    g.m_tiles = (int)p->m_tiles;
+    g.n_tiles = p->n_tiles;
+    g.Mout = (int)p->Mout;
+    g.kpad = (int)p->kpad;
+    g.kblocks = (int)(p->kpad / 32);
+    g.bn = p->bn;
+    g.flush = p->flush;
+    g.groups = (int)p->groups;
+    g.idesc = rts_ptx::idesc_f16(p->fp16, G_BM, p->bn);
+    g.bias = rts_group_bias(ctx, p->fp16, p->flush);
+    g.fp16 = p->fp16 ? 1 : 0;
+    g.cur = p->cur;
+    g.relax = relaxes(p, relax) ? 1 : 0;
+    g.residual = p->S32 != nullptr ? 1 : 0;
+    g.rs = p->fp16 ? p->rs : nullptr;
+    g.rs_inv = p->fp16 ? p->rs + p->rows_pad : nullptr;
+    g.cs_inv = p->fp16 ? p->cs + p->mpad : nullptr;
+    g.B = p->use_B ? p->B : nullptr;
+    g.lam = p->lam;
+    g.S32 = p->S32;
+    g.S64 = p->S64;
+    g.a[0] = p->a[0];
+    g.a[1] = p->a[1] ? p->a[1] : p->a[0];
+    g.resid = b->d_resid + i;
+    p->slot = (int)i;
+    tiles += p->m_tiles * p->n_tiles;
+}
+
+// Device table and residual slots for at least n problems.
+static int ensure_table(rts_batch* b, size_t n, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    if (n <= b->table_cap) return RTS_OK;
+    cudaStreamSynchronize(st);
+    rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));
+    rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
+    b->d_table = nullptr;
+    b->d_resid = nullptr;
+    b->table_cap = b->resid_cap = 0;
+    const size_t cap = std::max<size_t>(16, n * 2);
+    void* q;
+    int rc = rts_dmalloc(ctx, &q, cap * sizeof(GroupProblem), "batch table");
+    if (rc != RTS_OK) return rc;
+    b->d_table = (GroupProblem*)q;
+    rc = rts_dmalloc(ctx, &q, cap * sizeof(unsigned long long), "batch residuals");
+    if (rc != RTS_OK) return rc;
+    b->d_resid = (unsigned long long*)q;
+    b->table_cap = b->resid_cap = cap;
+    return RTS_OK;
 }
 
 // Build the device table for the next launch(es).
@@ -286,64 +363,11 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
     rts_ctx* ctx = b->ctx;
     if (!b->dirty && b->table_relax == relax && b->table_epoch == ctx->tuning_epoch) return RTS_OK;
     const size_t n = b->probs.size();
-    if (n > b->table_cap) {
-        cudaStreamSynchronize(st);
-        rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));
-        rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
-        b->d_table = nullptr;
-        b->d_resid = nullptr;
-        b->table_cap = b->resid_cap = 0;
-        const size_t cap = std::max<size_t>(16, n * 2);
-        void* q;
-        int rc = rts_dmalloc(ctx, &q, cap * sizeof(GroupProblem), "batch table");
-        if (rc != RTS_OK) return rc;
-        b->d_table = (GroupProblem*)q;
-        rc = rts_dmalloc(ctx, &q, cap * sizeof(unsigned long long), "batch residuals");
-        if (rc != RTS_OK) return rc;
-        b->d_resid = (unsigned long long*)q;
-        b->table_cap = b->resid_cap = cap;
-    }
+    int rc = ensure_table(b, n, st);
+    if (rc != RTS_OK) return rc;
     b->h_table.assign(n, GroupProblem());
     int64_t tiles = 0;
-    for (size_t i = 0; i < n; ++i) {
-        GProb* p = b->probs[i];
-        GroupProblem& g = b->h_table[i];
-        memset(&g, 0, sizeof(g));
-        memcpy(&g.mapA[0], p->maps[0], 128);
-        memcpy(&g.mapA[1], p->maps[1], 128);
-        memcpy(&g.mapW, p->maps[2], 128);
-        g.N = p->N;
-        g.ldS = p->ldS > 0 ? p->ldS : p->N;
-        g.rows = p->rows;
-        g.tile_begin = tiles;
-        g.m_tiles = (int)p->m_tiles;
-        g.n_tiles = p->n_tiles;
-        g.Mout = (int)p->Mout;
-        g.kpad = (int)p->kpad;
-        g.kblocks = (int)(p->kpad / 32);
-        g.bn = p->bn;
-        g.flush = p->flush;
-        g.groups = (int)p->groups;
-        g.idesc = rts_ptx::idesc_f16(p->fp16, G_BM, p->bn);
-        g.bias = rts_group_bias(ctx, p->fp16, p->flush);
-        g.fp16 = p->fp16 ? 1 : 0;
-        g.cur = p->cur;
-        const bool iterative = p->S32 != nullptr;
-        g.relax = (iterative && relax && p->a[1] && p->Mout == p->M) ? 1 : 0;
-        g.residual = iterative ? 1 : 0;
-        g.rs = p->fp16 ? p->rs : nullptr;
-        g.rs_inv = p->fp16 ? p->rs + p->rows_pad : nullptr;
-        g.cs_inv = p->fp16 ? p->cs + p->mpad : nullptr;
-        g.B = p->use_B ? p->B : nullptr;
-        g.lam = p->lam;
-        g.S32 = p->S32;
-        g.S64 = p->S64;
-        g.a[0] = p->a[0];
-        g.a[1] = p->a[1] ? p->a[1] : p->a[0];
-        g.resid = b->d_resid + i;
-        p->slot = (int)i;
-        tiles += p->m_tiles * p->n_tiles;
-    }
+    for (size_t i = 0; i < n; ++i) fill_entry(b, b->probs[i], relax, i, tiles, b->h_table[i]);
     b->total_tiles = tiles;
     if (n) RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_table.data(), n * sizeof(GroupProblem),
                                              cudaMemcpyHostToDevice, st));
@@ -363,10 +387,9 @@ int rts_group_prepare(rts_batch* b, int relax, cudaStream_t st)
     return upload_table(b, relax, st);
 }
 
-static int enqueue_step(rts_batch* b, int relax, cudaStream_t st)
+static int enqueue_step(rts_batch* b, int relax, cudaStream_t st, int n)
 {
     rts_ctx* ctx = b->ctx;
-    const int n = (int)b->probs.size();
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(b->d_resid, 0, n * sizeof(unsigned long long), st));
     const int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * G_CTAS_PER_SM, b->total_tiles);
     if (grid > 0) {
@@ -405,11 +428,65 @@ int rts_group_step(rts_batch* b, int relax, cudaStream_t st)
     RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
     int rc = upload_table(b, relax, st);
     if (rc != RTS_OK) return rc;
-    rc = enqueue_step(b, relax, st);
+    rc = enqueue_step(b, relax, st, (int)b->probs.size());
     if (rc != RTS_OK) return rc;
     host_flip(b, relax, 1);
     b->steps++;
     return RTS_OK;
+}
+
+// One step of a subset of the batch's problems (the others keep their state):
+// the table is rebuilt for the subset in a pinned host buffer (two, used in
+// turn) and copied without a host synchronisation.
+int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cudaStream_t st)
+{
+    rts_ctx* ctx = b->ctx;
+    RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell device");
+    if (n <= 0) return RTS_OK;
+    std::vector<GProb*> sel((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        sel[i] = rts_group_find(b, ids[i], nullptr);
+        RTS_REQUIRE(ctx, sel[i], RTS_ERR_INVALID_ARGUMENT, "no problem with id %lld in the batch", (long long)ids[i]);
+    }
+    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    int rc = ensure_table(b, (size_t)n, st);
+    if (rc != RTS_OK) return rc;
+    if (b->pin_cap < (size_t)n) {
+        for (int k = 0; k < 2; ++k) {
+            if (b->pin_ev[k]) cudaEventSynchronize(b->pin_ev[k]);
+            if (b->h_pin[k]) cudaFreeHost(b->h_pin[k]);
+            b->h_pin[k] = nullptr;
+        }
+        b->pin_cap = 0;
+        const size_t cap = std::max<size_t>(16, (size_t)n * 2);
+        for (int k = 0; k < 2; ++k) {
+            RTS_CUDA_TRY(ctx, cudaMallocHost(&b->h_pin[k], cap * sizeof(GroupProblem)));
+            if (!b->pin_ev[k]) RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&b->pin_ev[k], cudaEventDisableTiming));
+        }
+        b->pin_cap = cap;
+    }
+    const int k = b->pin_next;
+    b->pin_next ^= 1;
+    RTS_CUDA_TRY(ctx, cudaEventSynchronize(b->pin_ev[k]));  // its previous copy has been consumed
+    int64_t tiles = 0;
+    for (int i = 0; i < n; ++i) fill_entry(b, sel[i], relax, (size_t)i, tiles, b->h_pin[k][i]);
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_pin[k], (size_t)n * sizeof(GroupProblem),
+                                      cudaMemcpyHostToDevice, st));
+    RTS_CUDA_TRY(ctx, cudaEventRecord(b->pin_ev[k], st));
+    b->total_tiles = tiles;
+    b->dirty = true;  // the device table no longer holds the whole batch
+    rc = enqueue_step(b, relax, st, n);
+    if (rc != RTS_OK) return rc;
+    for (GProb* p : sel)
+        if (relaxes(p, relax)) p->cur ^= 1;
+    b->steps++;
+    return RTS_OK;
+}
+
+int64_t rts_group_problem_tiles(rts_batch* b, int64_t id)
+{
+    GProb* p = rts_group_find(b, id, nullptr);
+    return p ? p->m_tiles * p->n_tiles : 0;
 }
 
 int rts_group_capture(rts_batch* b, int steps, int relax)
@@ -427,7 +504,7 @@ int rts_group_capture(rts_batch* b, int steps, int relax)
     ctx->timing = false;  // no event records inside the graph
     RTS_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const int64_t launches0 = ctx->launches;
-    for (int s = 0; s < steps && rc == RTS_OK; ++s) rc = enqueue_step(b, relax, st);
+    for (int s = 0; s < steps && rc == RTS_OK; ++s) rc = enqueue_step(b, relax, st, (int)b->probs.size());
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     ctx->timing = was_timing;

@@ -106,6 +106,8 @@ struct rts_ctx {
     int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
     int tuning_epoch = 0;        // bumped when a setting that batch tables copy changes
     int64_t w_version = 0;       // bumped whenever d_W is rewritten
+    int serve_policy = 1;        // rts_serve_run: 0 all resident, 1 earliest deadline first, 2 least remaining work first
+    int64_t serve_budget = 0;    // tiles per step for policy 1 (0: 8 waves of the SMs)
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context

@@ -5,9 +5,14 @@
 //   * admission: arrived requests join the batch in arrival order as long as
 //     the context's device bytes plus the request's resident footprint stay
 //     under the HBM cap; a request larger than the cap is rejected;
-//   * every step advances every resident request by one source iteration in
-//     one grouped tcgen05 launch, so requests that arrive while others run
-//     share the device from their first step on;
+//   * every step advances resident requests by one source iteration in one
+//     grouped tcgen05 launch, so requests that arrive while others run share
+//     the device from their first step on.  Which ones (RTS_TUNE_SERVE_POLICY):
+//     earliest deadline first (deadline = arrival + 2 x the request's
+//     estimated solve time alone: iterations x (launch overhead + its tiles'
+//     waves on the SMs)), or least remaining work first (priority = remaining
+//     work / (1 + steps waited)), each up to a tile budget that keeps the
+//     step short; or all of them;
 //   * a request that has run its iterations is read back (S, FP32) and
 //     leaves the batch, freeing its memory for waiting requests.
 // Latency = completion time - arrival time (host wall clock).  Waits on the
@@ -48,7 +53,21 @@ struct Active {
     int64_t id = 0;
     int remaining = 0;
     int64_t bytes = 0;
+    int64_t tiles = 0;    // tiles of one step
+    double step_work = 0;  // cells x directions^2 of one step
+    int waited = 0;       // consecutive steps left out
+    double deadline = 0;  // arrival + 2 x estimated isolated solve time (s)
 };
+
+// Solve time of a request alone: per step a fixed launch and host overhead
+// plus its tiles in waves over the SMs, each tile taking about 1 us per
+// 32-direction K-slice (two issuers, measured on GB300 at N = 256 columns).
+double isolated_estimate(int64_t tiles, int64_t M, int iterations, int num_sms)
+{
+    const double waves = std::ceil((double)tiles / (double)num_sms);
+    const double tile_s = 1.0e-6 * (double)((M + 31) / 32);
+    return (double)iterations * (30e-6 + waves * tile_s);
+}
 
 }  // namespace
 
@@ -108,7 +127,11 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
                 rts_batch_destroy(batch);
                 return rc;
             }
-            active.push_back(Active{r, id, reqs[r].iterations, fp});
+            const int64_t tiles = rts_group_problem_tiles(batch, id);
+            active.push_back(Active{r, id, reqs[r].iterations, fp, tiles,
+                                    (double)d.N * (double)d.groups * (double)d.M * (double)d.M, 0,
+                                    reqs[r].arrival_s + 2.0 * isolated_estimate(tiles, d.M, reqs[r].iterations,
+                                                                                  ctx->num_sms)});
             waiting.pop_front();
             peak = std::max(peak, ctx->used_bytes);
         }
@@ -121,7 +144,34 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             }
             break;  // only rejected requests were left
         }
-        rc = rts_batch_step(batch, 1);
+        // the requests this step advances
+        std::vector<size_t> order(active.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::vector<char> in(active.size(), 1);
+        if (ctx->serve_policy != 0 && active.size() > 1) {
+            auto key = [&](size_t i) {
+                if (ctx->serve_policy == 1) return active[i].deadline;
+                return active[i].step_work * active[i].remaining / (1.0 + active[i].waited);
+            };
+            std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return key(x) < key(y); });
+            const int64_t budget = ctx->serve_budget > 0 ? ctx->serve_budget : 8 * (int64_t)ctx->num_sms;
+            int64_t used = 0;
+            for (size_t o = 0; o < order.size(); ++o) {
+                const size_t i = order[o];
+                in[i] = (o == 0 || used + active[i].tiles <= budget) ? 1 : 0;
+                if (in[i]) used += active[i].tiles;
+            }
+        }
+        std::vector<int64_t> ids;
+        for (size_t i = 0; i < active.size(); ++i) {
+            if (in[i]) {
+                ids.push_back(active[i].id);
+                active[i].waited = 0;
+            } else {
+                active[i].waited++;
+            }
+        }
+        rc = rts_group_step_subset(batch, 1, ids.data(), (int)ids.size(), ctx->streams[RTS_STREAM_SCATTERING_1]);
         if (rc == RTS_OK) rc = rts_batch_sync(batch, step_timeout_us);
         if (rc != RTS_OK) {
             rts_batch_destroy(batch);
@@ -131,7 +181,7 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
         // completions
         for (size_t i = 0; i < active.size();) {
             Active& a = active[i];
-            if (--a.remaining > 0) {
+            if (a.waited > 0 || --a.remaining > 0) {
                 ++i;
                 continue;
             }

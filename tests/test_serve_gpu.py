@@ -28,11 +28,17 @@ def make_requests(shapes, arrivals, iters, seed=0):
     return reqs, keep
 
 
-def test_serving_results_equal_isolated_solves(ctx):
+@pytest.mark.parametrize("policy,budget", [(1, 0), (1, 24), (2, 24), (0, 0)])
+def test_serving_results_equal_isolated_solves(ctx, policy, budget):
+    """Every policy (least remaining work first, with the default budget and
+    with one so small that most steps advance a subset; all resident) gives
+    each request exactly its isolated result."""
     shapes = [(3000, 110, 0.2), (5000, 302, 0.5), (2000, 590, 0.7), (4000, 146, 0.0), (2500, 302, 0.8)]
     arrivals = [0.0, 0.0, 0.002, 0.004, 0.006]
     iters = [5, 8, 6, 7, 5]
     reqs, keep = make_requests(shapes, arrivals, iters)
+    ctx.set_tuning(_native.TUNE_SERVE_POLICY, policy)
+    ctx.set_tuning(_native.TUNE_SERVE_BUDGET, budget)
     stats, lat = serve(ctx, reqs, hbm_cap=ctx.hbm_used() + (8 << 30))
     assert stats.completed == len(reqs) and stats.rejected == 0
     assert stats.max_active >= 2  # requests overlapped on the device
