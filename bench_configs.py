@@ -103,6 +103,7 @@ def timed_steps(ctx, fn, steps, torch, stream_handle):
 # ---------------------------------------------------------------- configurations
 def config3(pkg, native, ctx, torch, steps, warmup, precision):
     N, M, G, g = 300_000, 590, 8, 0.7
+    tuned = ctx.autotune(M, precision)  # tile width for M = 590 (not timed)
     lam = np.array([0.3 + 0.08 * i for i in range(G)])
     desc = native.problem_desc(N, M, G, 1, g, precision)
     b = native.Batch(ctx)
@@ -122,7 +123,8 @@ def config3(pkg, native, ctx, torch, steps, warmup, precision):
             "tflops_alg": 2.0 * N * G * M * M / (kms / max(kn, 1) / 1e3) / 1e12,
             "max_rel_err": mx, "mean_rel_err": mean, "precision": precision,
             "workload": "300,000 cells x 590 directions x 8 groups, HG g=0.7 row-normalised, lognormal(0,1) FP32, "
-                        "lambda_g=0.3+0.08g"}
+                        "lambda_g=0.3+0.08g",
+            "autotuned_bn": tuned[0], "autotune_ms": {str(k): v for k, v in tuned[2].items()}}
 
 
 def config4_problems(seed=3):
@@ -140,6 +142,7 @@ def config4_problems(seed=3):
 
 def config4(pkg, native, ctx, torch, steps, warmup, precision):
     probs = config4_problems()
+    tuned = {M: ctx.autotune(M, precision)[0] for M in sorted({p[1] for p in probs})}  # not timed
     b = native.Batch(ctx)
     ids = []
     for (N, M, ph, g, lam, seed) in probs:
@@ -172,7 +175,7 @@ def config4(pkg, native, ctx, torch, steps, warmup, precision):
     return {"value": units * nsteps / t / 1e9, "ms_per_step": t / nsteps * 1e3, "problems": nprob, "tiles": tiles,
             "tflops_alg": flops * nsteps / t / 1e12, "graph_steps": per_graph, "gpu_launches": launches,
             "max_rel_err": max(e[0] for e in errs), "mean_rel_err": float(np.mean([e[1] for e in errs])),
-            "precision": precision,
+            "precision": precision, "autotuned_bn": {str(k): v for k, v in tuned.items()},
             "workload": "64 problems, N log-uniform [5k,200k], M in {146,302,590}, Thomson or HG g~U[0,0.8], "
                         "lambda~U[0.2,0.95], seed 3; one grouped launch per step, CUDA-graph replay"}
 
@@ -246,14 +249,19 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
         row = {"load": f, "offered_load": offered, "rate_per_s": rate, "requests": len(reqs), "completed": st.completed,
                "rejected": st.rejected, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
                "throughput_cell_dir_iter_per_s": st.throughput, "max_active": st.max_active,
+               "makespan_s": st.makespan_s, "host_admit_s": st.admit_s, "device_step_s": st.step_s,
+               "host_retire_s": st.retire_s, "steps": st.steps,
                "peak_gb": st.peak_bytes / 1e9}
         if abs(f - 0.8) < 1e-9:
-            # isolated solve time of every request of this run, alone on the device
+            # isolated solve time of every request of this run, alone on the
+            # device, one whole step per launch
+            ctx.set_tuning(native.TUNE_SERVE_POLICY, 0)
             iso = []
             for r in reqs:
                 s1, l1 = native.serve(ctx, [native.Request(0.0, r.desc, r.iterations, r.ibar, r.B, r.lambda_, None)],
                                       cap)
                 iso.append(l1[0])
+            ctx.set_tuning(native.TUNE_SERVE_POLICY, policy)
             iso = np.array(iso)
             ratio = ok / iso[: len(ok)] if len(ok) == len(iso) else lat / iso
             row["isolated_p50_ms"] = float(np.percentile(iso, 50))

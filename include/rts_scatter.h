@@ -338,6 +338,7 @@ typedef struct rts_serve_stats {
     double makespan_s;
     double throughput;      /* cell-direction-iterations per second */
     double p50_ms, p99_ms, mean_ms, max_ms;
+    double admit_s, step_s, retire_s;  /* host time in admission (set-up), device steps, retirement */
 } rts_serve_stats;
 
 /* Runs the requests through one device batch with continuous batching:
@@ -433,6 +434,20 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
 #define RTS_TUNE_SERVE_POLICY 3
 #define RTS_TUNE_SERVE_BUDGET 4
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
+
+/* Autotuner of the tensor-core kernel's tile width (out-directions per
+ * tile).  Times every distinct tiling of M directions (tiles of 64..256) on a
+ * synthetic problem of `cells` cells (0: four waves of row tiles), keeps the
+ * fastest in the context's table and reports it; problems created with
+ * bn = 0 and M directions at that precision and flush then use it.  tried_bn
+ * / tried_ms (capacity entries, may be NULL) receive every timing, *tried
+ * their count.  Results do not depend on the tile width (same arithmetic per
+ * output).  No counterpart in the reference. */
+int rts_autotune(rts_ctx* ctx, int64_t M, int precision, int flush, int64_t cells, int* best_bn, double* best_ms,
+                 int* tried_bn, double* tried_ms, int capacity, int* tried);
+/* The table as text ("M precision flush bn ms" per line), and back. */
+int rts_autotune_save(rts_ctx* ctx, const char* path);
+int rts_autotune_load(rts_ctx* ctx, const char* path);
 
 /* The cudaStream_t of a stream slot (for callers that order their own work
  * or record CUDA events against the library's streams). */

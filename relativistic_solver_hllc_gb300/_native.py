@@ -110,6 +110,10 @@ _SIGNATURES = {
     "rts_write_simple_bin": (C.c_int, [C.c_char_p, _i64, _i64, _vp]),
     "rts_partition": (C.c_int, [C.c_int, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
     "rts_set_tuning": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "rts_autotune": (C.c_int, [_vp, _i64, C.c_int, C.c_int, _i64, C.POINTER(C.c_int), _dp, C.POINTER(C.c_int), _dp,
+                               C.c_int, C.POINTER(C.c_int)]),
+    "rts_autotune_save": (C.c_int, [_vp, C.c_char_p]),
+    "rts_autotune_load": (C.c_int, [_vp, C.c_char_p]),
     "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "rts_launch_count": (C.c_int, [_vp, C.POINTER(_i64)]),
     "rts_kernel_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(_i64)]),
@@ -493,6 +497,23 @@ class Context:
     def set_tuning(self, key: int, value: int):
         self._check(self.lib.rts_set_tuning(self.h, int(key), int(value)), "rts_set_tuning")
 
+    def autotune(self, M: int, precision="fp16x3", flush: int = 0, cells: int = 0):
+        """Best tile width for M directions; returns (bn, ms, {bn: ms})."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        best, tried = C.c_int(), C.c_int()
+        best_ms = C.c_double()
+        bns = (C.c_int * 16)()
+        mss = (C.c_double * 16)()
+        self._check(self.lib.rts_autotune(self.h, int(M), prec, int(flush), int(cells), C.byref(best), C.byref(best_ms),
+                                          bns, mss, 16, C.byref(tried)), "rts_autotune")
+        return best.value, best_ms.value, {bns[i]: mss[i] for i in range(min(tried.value, 16))}
+
+    def autotune_save(self, path):
+        self._check(self.lib.rts_autotune_save(self.h, str(path).encode()), "rts_autotune_save")
+
+    def autotune_load(self, path):
+        self._check(self.lib.rts_autotune_load(self.h, str(path).encode()), "rts_autotune_load")
+
     def stream_handle(self, stream: int) -> int:
         v = _vp()
         self._check(self.lib.rts_stream_handle(self.h, int(stream), C.byref(v)), "rts_stream_handle")
@@ -635,7 +656,8 @@ class ServeStats(C.Structure):
     """rts_serve_stats"""
     _fields_ = [("completed", C.c_int64), ("rejected", C.c_int64), ("max_active", C.c_int64), ("steps", C.c_int64),
                 ("peak_bytes", C.c_int64), ("makespan_s", C.c_double), ("throughput", C.c_double),
-                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double)]
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("admit_s", C.c_double), ("step_s", C.c_double), ("retire_s", C.c_double)]
 
 
 _SIGNATURES.update({

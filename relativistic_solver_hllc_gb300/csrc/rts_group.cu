@@ -200,6 +200,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     p->rows = N * groups;
     p->fp16 = fp16;
     p->flush = std::min(std::max(flush, 1), G_MAX_FLUSH);
+    if (bn_override <= 0 && Mout == Min) bn_override = rts_tuned_bn(ctx, Min, fp16, p->flush);  // 0 if not tuned
     rts_group_geometry(Min, Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad, &p->rows_pad,
                        &p->m_tiles);
     int rc;
@@ -319,6 +320,8 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.fp16 = p->fp16 ? 1 : 0;
     g.cur = p->cur;
     g.relax = relaxes(p, relax) ? 1 : 0;
+    g.flip = g.relax;
+    g.tile_off = 0;
     g.residual = p->S32 != nullptr ? 1 : 0;
     g.rs = p->fp16 ? p->rs : nullptr;
     g.rs_inv = p->fp16 ? p->rs + p->rows_pad : nullptr;
@@ -435,10 +438,14 @@ int rts_group_step(rts_batch* b, int relax, cudaStream_t st)
     return RTS_OK;
 }
 
-// One step of a subset of the batch's problems (the others keep their state):
-// the table is rebuilt for the subset in a pinned host buffer (two, used in
-// turn) and copied without a host synchronisation.
-int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cudaStream_t st)
+// Part of a step of some of the batch's problems (the others keep their
+// state): problem ids[i] runs tiles [first[i], first[i] + count[i]) of its
+// current step, and its step ends in this launch when that range reaches its
+// last tile (then, relaxing, its Ibar buffers flip).  The table is rebuilt
+// for these pieces in a pinned host buffer (two, used in turn) and copied
+// without a host synchronisation.  Residuals are those of this launch's tiles.
+int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int64_t* first, const int64_t* count,
+                          int n, cudaStream_t st)
 {
     rts_ctx* ctx = b->ctx;
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell device");
@@ -447,6 +454,10 @@ int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cu
     for (int i = 0; i < n; ++i) {
         sel[i] = rts_group_find(b, ids[i], nullptr);
         RTS_REQUIRE(ctx, sel[i], RTS_ERR_INVALID_ARGUMENT, "no problem with id %lld in the batch", (long long)ids[i]);
+        const int64_t tiles = sel[i]->m_tiles * sel[i]->n_tiles;
+        const int64_t f = first ? first[i] : 0, c = count ? count[i] : tiles;
+        RTS_REQUIRE(ctx, f >= 0 && c > 0 && f + c <= tiles, RTS_ERR_INVALID_ARGUMENT,
+                    "tiles [%lld,%lld) outside the problem's %lld", (long long)f, (long long)(f + c), (long long)tiles);
     }
     RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
     int rc = ensure_table(b, (size_t)n, st);
@@ -468,19 +479,37 @@ int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cu
     const int k = b->pin_next;
     b->pin_next ^= 1;
     RTS_CUDA_TRY(ctx, cudaEventSynchronize(b->pin_ev[k]));  // its previous copy has been consumed
-    int64_t tiles = 0;
-    for (int i = 0; i < n; ++i) fill_entry(b, sel[i], relax, (size_t)i, tiles, b->h_pin[k][i]);
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        GroupProblem& g = b->h_pin[k][i];
+        int64_t ignored = 0;
+        fill_entry(b, sel[i], relax, (size_t)i, ignored, g);
+        const int64_t tiles = sel[i]->m_tiles * sel[i]->n_tiles;
+        const int64_t f = first ? first[i] : 0, c = count ? count[i] : tiles;
+        g.tile_begin = total;
+        g.tile_off = f;
+        g.flip = (g.relax && f + c == tiles) ? 1 : 0;
+        total += c;
+    }
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_pin[k], (size_t)n * sizeof(GroupProblem),
                                       cudaMemcpyHostToDevice, st));
     RTS_CUDA_TRY(ctx, cudaEventRecord(b->pin_ev[k], st));
-    b->total_tiles = tiles;
+    b->total_tiles = total;
     b->dirty = true;  // the device table no longer holds the whole batch
     rc = enqueue_step(b, relax, st, n);
     if (rc != RTS_OK) return rc;
-    for (GProb* p : sel)
-        if (relaxes(p, relax)) p->cur ^= 1;
+    for (int i = 0; i < n; ++i) {
+        const int64_t tiles = sel[i]->m_tiles * sel[i]->n_tiles;
+        const int64_t f = first ? first[i] : 0, c = count ? count[i] : tiles;
+        if (relaxes(sel[i], relax) && f + c == tiles) sel[i]->cur ^= 1;
+    }
     b->steps++;
     return RTS_OK;
+}
+
+int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cudaStream_t st)
+{
+    return rts_group_step_pieces(b, relax, ids, nullptr, nullptr, n, st);
 }
 
 int64_t rts_group_problem_tiles(rts_batch* b, int64_t id)

@@ -50,6 +50,8 @@ int rts_group_step(rts_batch* b, int relax, cudaStream_t st);
 // then queues its launch without a host synchronisation).
 int rts_group_prepare(rts_batch* b, int relax, cudaStream_t st);
 int rts_group_step_subset(rts_batch* b, int relax, const int64_t* ids, int n, cudaStream_t st);
+int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int64_t* first, const int64_t* count,
+                          int n, cudaStream_t st);
 int64_t rts_group_problem_tiles(rts_batch* b, int64_t id);
 int rts_group_capture(rts_batch* b, int steps, int relax);
 int rts_group_replay(rts_batch* b);

@@ -62,7 +62,8 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     int64_t N;            // cells per group
     int64_t ldS;          // row pitch of S32 / S64 in cells (>= N; N unless the output is a cell range of a wider S)
     int64_t rows;         // groups * N
-    int64_t tile_begin;   // first global tile index of this problem
+    int64_t tile_begin;   // first global tile index of this problem in the launch
+    int64_t tile_off;     // the problem's own first tile in this launch (a step may span launches)
     int m_tiles, n_tiles;
     int Mout, kpad, kblocks, bn, flush, groups;
     uint32_t idesc;
@@ -70,6 +71,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     int fp16;
     int cur;              // buffer holding the current Ibar
     int relax, residual;
+    int flip;             // the step ends in this launch: flip the ping-pong Ibar buffer after it
     const float* rs;      // [rows_pad] row scales (FP16 mode) or null
     const float* rs_inv;
     const float* cs_inv;  // [mpad] column unscale (FP16 mode) or null
@@ -161,7 +163,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             bool ok = true;
             for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
                 const GroupProblem& P = probs[find_problem(probs, nprob, t)];
-                const int64_t lt = t - P.tile_begin;
+                const int64_t lt = t - P.tile_begin + P.tile_off;
                 const int n_tiles = P.n_tiles, nkb = P.kblocks, bn = P.bn;
                 const int m0 = (int)(lt / n_tiles) * G_BM, n0 = (int)(lt % n_tiles) * bn;
                 const void* mapA = &P.mapA[P.cur];
@@ -250,7 +252,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const int nkb = P.kblocks, flush = P.flush, bn = P.bn;
             const int nchunks = (nkb + flush - 1) / flush;
             const int ncols = min(64, bn - 64 * cs);  // columns of this warp (multiple of 16; <= 0: none)
-            const int64_t lt = t - P.tile_begin;
+            const int64_t lt = t - P.tile_begin + P.tile_off;
             const int m_tile = (int)(lt / P.n_tiles), n_tile = (int)(lt % P.n_tiles);
             float run[64];
 #pragma unroll
@@ -473,10 +475,11 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     }
 }
 
-// Flip the ping-pong Ibar buffer of every relaxing problem (launched after
-// the step so that a captured graph replays step after step on device).
+// Flip the ping-pong Ibar buffer of every problem whose relaxed step ended in
+// this launch (launched after it, so that a captured graph replays step after
+// step on the device).
 __global__ void group_flip_kernel(GroupProblem* probs, int nprob)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nprob && probs[p].relax) probs[p].cur ^= 1;
+    if (p < nprob && probs[p].flip) probs[p].cur ^= 1;
 }

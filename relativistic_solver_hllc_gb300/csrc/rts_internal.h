@@ -43,6 +43,12 @@ constexpr int64_t RTS_RESID_CAP = 4096;
 struct rts_batch;
 constexpr int RTS_HOST_CHUNKS = 8;  // cell ranges of a pipelined host-buffer call
 
+struct rts_tune_entry {  // autotuned tile width of the tensor-core kernel
+    int64_t M = 0;
+    int precision = 0, flush = 1, bn = 0;
+    double ms = 0.0;
+};
+
 struct rts_split_state {
     int precision = -1;             // precision of the resident source iteration
     rts_batch* iter = nullptr;      // one-problem batch of the source iteration
@@ -108,6 +114,7 @@ struct rts_ctx {
     int64_t w_version = 0;       // bumped whenever d_W is rewritten
     int serve_policy = 1;        // rts_serve_run: 0 all resident, 1 earliest deadline first, 2 least remaining work first
     int64_t serve_budget = 0;    // tiles per step for policy 1 (0: 8 waves of the SMs)
+    std::vector<rts_tune_entry> tune;  // rts_autotune results, used for problems created with bn = 0
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context
@@ -153,6 +160,7 @@ int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaSt
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 
 // Tensor-core path (rts_split.cu).
+int rts_tuned_bn(const rts_ctx* ctx, int64_t M, bool fp16, int flush);
 int rts_split_setup(rts_ctx* ctx, int precision);
 int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
 // One evaluation from the device Illum (faces) into the FP64 device S, with

@@ -11,8 +11,10 @@
 //     earliest deadline first (deadline = arrival + 2 x the request's
 //     estimated solve time alone: iterations x (launch overhead + its tiles'
 //     waves on the SMs)), or least remaining work first (priority = remaining
-//     work / (1 + steps waited)), each up to a tile budget that keeps the
-//     step short; or all of them;
+//     work / (1 + steps waited)), each filling a tile budget per launch that
+//     keeps launches short -- a request's step is cut into pieces of tiles
+//     when it does not fit, so a large step never holds back an urgent small
+//     request for long; or all of them, one whole step each;
 //   * a request that has run its iterations is read back (S, FP32) and
 //     leaves the batch, freeing its memory for waiting requests.
 // Latency = completion time - arrival time (host wall clock).  Waits on the
@@ -57,6 +59,7 @@ struct Active {
     double step_work = 0;  // cells x directions^2 of one step
     int waited = 0;       // consecutive steps left out
     double deadline = 0;  // arrival + 2 x estimated isolated solve time (s)
+    int64_t pos = 0;      // next tile of the current step (a step may span launches)
 };
 
 // Solve time of a request alone: per step a fixed launch and host overhead
@@ -93,6 +96,7 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
     std::vector<double> lat;
     int64_t next = 0, done = 0, rejected = 0, steps = 0, peak = ctx->used_bytes, max_active = 0;
     double work = 0.0;  // cell-direction-iterations completed
+    double admit_s = 0.0, step_s = 0.0, retire_s = 0.0;
     const int64_t base_bytes = ctx->used_bytes;
     const auto t0 = clock_type::now();
 
@@ -114,7 +118,9 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             }
             if (ctx->used_bytes + fp + scratch > hbm_cap && !active.empty()) break;
             int64_t id = 0;
+            const double ta = seconds_since(t0);
             rc = rts_batch_add(batch, &d, reqs[r].ibar, reqs[r].B, reqs[r].lambda, &id);
+            admit_s += seconds_since(t0) - ta;
             if (rc == RTS_ERR_OVER_BUDGET || rc == RTS_ERR_OUT_OF_MEMORY) {
                 if (active.empty()) {  // nothing will free memory: reject
                     waiting.pop_front();
@@ -144,50 +150,66 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             }
             break;  // only rejected requests were left
         }
-        // the requests this step advances
+        // the pieces this launch runs: (request, first tile, tiles)
         std::vector<size_t> order(active.size());
         for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-        std::vector<char> in(active.size(), 1);
-        if (ctx->serve_policy != 0 && active.size() > 1) {
+        std::vector<int64_t> take(active.size(), 0);
+        if (ctx->serve_policy != 0) {
             auto key = [&](size_t i) {
                 if (ctx->serve_policy == 1) return active[i].deadline;
                 return active[i].step_work * active[i].remaining / (1.0 + active[i].waited);
             };
             std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return key(x) < key(y); });
             const int64_t budget = ctx->serve_budget > 0 ? ctx->serve_budget : 8 * (int64_t)ctx->num_sms;
-            int64_t used = 0;
-            for (size_t o = 0; o < order.size(); ++o) {
-                const size_t i = order[o];
-                in[i] = (o == 0 || used + active[i].tiles <= budget) ? 1 : 0;
-                if (in[i]) used += active[i].tiles;
+            int64_t left = budget;
+            for (size_t i : order) {
+                if (left <= 0) break;
+                take[i] = std::min(active[i].tiles - active[i].pos, left);
+                left -= take[i];
             }
+        } else {
+            for (size_t i = 0; i < active.size(); ++i) take[i] = active[i].tiles - active[i].pos;
         }
-        std::vector<int64_t> ids;
+        std::vector<int64_t> ids, first, count;
         for (size_t i = 0; i < active.size(); ++i) {
-            if (in[i]) {
+            if (take[i] > 0) {
                 ids.push_back(active[i].id);
+                first.push_back(active[i].pos);
+                count.push_back(take[i]);
                 active[i].waited = 0;
             } else {
                 active[i].waited++;
             }
         }
-        rc = rts_group_step_subset(batch, 1, ids.data(), (int)ids.size(), ctx->streams[RTS_STREAM_SCATTERING_1]);
+        const double ts = seconds_since(t0);
+        rc = rts_group_step_pieces(batch, 1, ids.data(), first.data(), count.data(), (int)ids.size(),
+                                   ctx->streams[RTS_STREAM_SCATTERING_1]);
         if (rc == RTS_OK) rc = rts_batch_sync(batch, step_timeout_us);
+        step_s += seconds_since(t0) - ts;
         if (rc != RTS_OK) {
             rts_batch_destroy(batch);
             return rc;
+        }
+        for (size_t i = 0; i < active.size(); ++i) {
+            active[i].pos += take[i];
+            if (take[i] > 0 && active[i].pos == active[i].tiles) {  // the step is complete
+                active[i].pos = 0;
+                active[i].remaining--;
+            }
         }
         ++steps;
         // completions
         for (size_t i = 0; i < active.size();) {
             Active& a = active[i];
-            if (a.waited > 0 || --a.remaining > 0) {
+            if (a.remaining > 0) {
                 ++i;
                 continue;
             }
             const rts_request& q = reqs[a.req];
+            const double tr = seconds_since(t0);
             rc = rts_batch_read(batch, a.id, q.S_out, nullptr);
             if (rc == RTS_OK) rc = rts_batch_remove(batch, a.id);
+            retire_s += seconds_since(t0) - tr;
             if (rc != RTS_OK) {
                 rts_batch_destroy(batch);
                 return rc;
@@ -219,6 +241,9 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
     stats->mean_ms = lat.empty() ? 0.0 : sum / (double)lat.size();
     stats->max_ms = mx;
     stats->peak_bytes = peak;
+    stats->admit_s = admit_s;
+    stats->step_s = step_s;
+    stats->retire_s = retire_s;
     return RTS_OK;
 }
 
