@@ -431,8 +431,11 @@ int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
  *   RTS_TUNE_SERVE_BUDGET: tiles (128 cells x up to 256 directions) per step
  *   under policies 1 and 2; 0 = 8 waves of the SMs.  At least one request
  *   always runs. */
+/*   RTS_TUNE_SERVE_SLACK: policy 1's deadline, arrival + slack/100 x the
+ *   request's estimated solve time alone (0 = 500). */
 #define RTS_TUNE_SERVE_POLICY 3
 #define RTS_TUNE_SERVE_BUDGET 4
+#define RTS_TUNE_SERVE_SLACK 5
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* Autotuner of the tensor-core kernel's tile width (out-directions per

@@ -62,6 +62,7 @@ TUNE_FLUSH = 1  # RTS_TUNE_FLUSH
 TUNE_BIAS = 2   # RTS_TUNE_BIAS
 TUNE_SERVE_POLICY = 3  # RTS_TUNE_SERVE_POLICY
 TUNE_SERVE_BUDGET = 4  # RTS_TUNE_SERVE_BUDGET
+TUNE_SERVE_SLACK = 5  # RTS_TUNE_SERVE_SLACK
 
 _dp = C.POINTER(C.c_double)
 _i64 = C.c_int64

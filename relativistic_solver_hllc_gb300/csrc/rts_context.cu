@@ -767,6 +767,10 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
         RTS_REQUIRE(ctx, value >= 0 && value <= 2, RTS_ERR_INVALID_ARGUMENT, "serving policy %d not 0, 1 or 2", value);
         ctx->serve_policy = value;
         return RTS_OK;
+    case RTS_TUNE_SERVE_SLACK:
+        RTS_REQUIRE(ctx, value >= 0 && value <= 100000, RTS_ERR_INVALID_ARGUMENT, "slack %d outside [0,100000]", value);
+        ctx->serve_slack = value > 0 ? value : 500;
+        return RTS_OK;
     case RTS_TUNE_SERVE_BUDGET:
         RTS_REQUIRE(ctx, value >= 0, RTS_ERR_INVALID_ARGUMENT, "tile budget %d below 0", value);
         ctx->serve_budget = value;

@@ -381,6 +381,21 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             };
             float rmax = 0.0f;
             bool overflow = false;
+            // previous S of a block of 8 columns, loaded one block ahead
+            auto load_old = [&](int e0, float (&o)[8]) {
+                const int k0 = kbase + e0;
+                const int nk = min(8, Mout - k0);
+                if (in_row && nk > 0 && residual && S && e0 < ncols) {
+                    const float* sp = S + (int64_t)k0 * ld;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j, sp += ld) o[j] = j < nk ? *sp : 0.0f;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) o[j] = 0.0f;
+                }
+            };
+            float old_next[8];
+            load_old(0, old_next);
             fetch(0, 0);
             cp_async_commit();
 #pragma unroll 1
@@ -391,16 +406,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 const bool rel = want_rel && nk > 0;  // same for all lanes
                 if (e0 + 8 < ncols) fetch(e0 + 8, (st + 1) & 1);
                 cp_async_commit();
-                // global loads first, then the TMEM read
                 float old[8];
-                if (live_k && residual && S) {
-                    const float* sp = S + (int64_t)k0 * ld;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j, sp += ld) old[j] = j < nk ? *sp : 0.0f;
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) old[j] = 0.0f;
-                }
+                for (int j = 0; j < 8; ++j) old[j] = old_next[j];
+                load_old(e0 + 8, old_next);
                 float cin[8];
                 if (fp16) {
                     const float4 c0 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0));

@@ -114,6 +114,7 @@ struct rts_ctx {
     int64_t w_version = 0;       // bumped whenever d_W is rewritten
     int serve_policy = 1;        // rts_serve_run: 0 all resident, 1 earliest deadline first, 2 least remaining work first
     int64_t serve_budget = 0;    // tiles per step for policy 1 (0: 8 waves of the SMs)
+    int serve_slack = 500;       // policy 1 deadline: arrival + serve_slack / 100 x estimated isolated time
     std::vector<rts_tune_entry> tune;  // rts_autotune results, used for problems created with bn = 0
 
     // instrumentation

@@ -8,9 +8,9 @@
 //   * every step advances resident requests by one source iteration in one
 //     grouped tcgen05 launch, so requests that arrive while others run share
 //     the device from their first step on.  Which ones (RTS_TUNE_SERVE_POLICY):
-//     earliest deadline first (deadline = arrival + 2 x the request's
-//     estimated solve time alone: iterations x (launch overhead + its tiles'
-//     waves on the SMs)), or least remaining work first (priority = remaining
+//     earliest deadline first (deadline = arrival + slack (default 5) x the
+//     request's estimated solve time alone: iterations x (launch overhead +
+//     its tiles' waves on the SMs)), or least remaining work first (priority = remaining
 //     work / (1 + steps waited)), each filling a tile budget per launch that
 //     keeps launches short -- a request's step is cut into pieces of tiles
 //     when it does not fit, so a large step never holds back an urgent small
@@ -136,8 +136,9 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             const int64_t tiles = rts_group_problem_tiles(batch, id);
             active.push_back(Active{r, id, reqs[r].iterations, fp, tiles,
                                     (double)d.N * (double)d.groups * (double)d.M * (double)d.M, 0,
-                                    reqs[r].arrival_s + 2.0 * isolated_estimate(tiles, d.M, reqs[r].iterations,
-                                                                                  ctx->num_sms)});
+                                    reqs[r].arrival_s + 0.01 * ctx->serve_slack *
+                                                            isolated_estimate(tiles, d.M, reqs[r].iterations,
+                                                                              ctx->num_sms)});
             waiting.pop_front();
             peak = std::max(peak, ctx->used_bytes);
         }
