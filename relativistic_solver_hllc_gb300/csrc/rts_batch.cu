@@ -62,6 +62,22 @@ int rts_batch_add(rts_batch* batch, const rts_problem_desc* d, const float* ibar
 {
     if (!batch) return RTS_ERR_INVALID_ARGUMENT;
     rts_ctx* ctx = rts_group_ctx(batch);
+    return rts_batch_add_on(batch, d, ibar, B, lambda, ctx->streams[RTS_STREAM_SCATTERING_1], true, id);
+}
+
+}  // extern "C"
+
+// Set-up of a new problem queued on `st`: directions, W, split W, the Ibar
+// copy and its split.  With sync the call returns once the problem is ready;
+// without, the caller must see work queued on `st` finish (an event recorded
+// after the call) before the problem's first step is launched on another
+// stream.  Host inputs are read during the call when pageable, or by the
+// queued copy when pinned (they must then stay valid until it has run).
+int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* ibar, const float* B,
+                     const double* lambda, cudaStream_t st, bool sync, int64_t* id)
+{
+    if (!batch) return RTS_ERR_INVALID_ARGUMENT;
+    rts_ctx* ctx = rts_group_ctx(batch);
     int rc = check_desc(ctx, d);
     if (rc != RTS_OK) return rc;
     RTS_REQUIRE(ctx, ibar && B && lambda, RTS_ERR_INVALID_ARGUMENT, "rts_batch_add: null input");
@@ -69,18 +85,17 @@ int rts_batch_add(rts_batch* batch, const rts_problem_desc* d, const float* ibar
     for (int64_t g = 0; g < G; ++g)
         RTS_REQUIRE(ctx, lambda[g] >= 0.0 && lambda[g] <= 1.0, RTS_ERR_INVALID_ARGUMENT,
                     "albedo %g of group %lld outside [0, 1]", lambda[g], (long long)g);
-    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
 
     // direction set and W in scratch, followed by the FP32 Ibar staging area
     std::vector<double> xyz(3 * (size_t)M), area((size_t)M);
     double full_area = 0.0;
     rts_synth_directions(M, xyz.data(), area.data(), &full_area);
     double *d_xyz = nullptr, *d_area = nullptr;
-    rc = rts_group_dirs(batch, xyz.data(), area.data(), M, &d_xyz, &d_area);
+    rc = rts_group_dirs(batch, xyz.data(), area.data(), M, &d_xyz, &d_area, st);
     if (rc != RTS_OK) return rc;
     const size_t w_bytes = (size_t)(M * M) * 8, i_bytes = (size_t)(rows * M) * 4;
     void* scratch = nullptr;
-    rc = rts_group_scratch(batch, w_bytes + i_bytes, &scratch);
+    rc = rts_group_scratch(batch, w_bytes + i_bytes, &scratch, st);
     if (rc != RTS_OK) return rc;
     double* W = static_cast<double*>(scratch);
     float* stage = reinterpret_cast<float*>(static_cast<char*>(scratch) + w_bytes);
@@ -88,7 +103,8 @@ int rts_batch_add(rts_batch* batch, const rts_problem_desc* d, const float* ibar
     if (rc != RTS_OK) return rc;
 
     GProb* p = nullptr;
-    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, d->precision == RTS_PREC_FP16X3, d->flush, d->bn, true, &p);
+    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, d->precision == RTS_PREC_FP16X3, d->flush, d->bn, true, &p,
+                               st);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
     for (int64_t g = 0; g < G; ++g) lam[(size_t)g] = (float)lambda[g];
@@ -98,23 +114,25 @@ int rts_batch_add(rts_batch* batch, const rts_problem_desc* d, const float* ibar
     if (e != cudaSuccess) {
         int64_t tmp = 0;
         rts_group_attach(batch, p, &tmp);  // owned by the batch from here; remove frees it
-        rts_group_remove(batch, tmp);
+        rts_group_remove_on(batch, tmp, st);
         return rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: copy failed: %s", cudaGetErrorString(e));
     }
     rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->fp16, p->rs, p->rows_pad, p->a[0], st);
-    if (rc == RTS_OK) {
+    if (rc == RTS_OK && sync) {
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: %s", cudaGetErrorString(e));
     }
     int64_t new_id = 0;
     rts_group_attach(batch, p, &new_id);
     if (rc != RTS_OK) {
-        rts_group_remove(batch, new_id);
+        rts_group_remove_on(batch, new_id, st);
         return rc;
     }
     if (id) *id = new_id;
     return RTS_OK;
 }
+
+extern "C" {
 
 int rts_batch_remove(rts_batch* batch, int64_t id)
 {

@@ -56,6 +56,42 @@ void rts_dfree(rts_ctx* ctx, void* p, size_t bytes)
     ctx->used_bytes -= (int64_t)bytes;
 }
 
+int rts_pmalloc(rts_ctx* ctx, void** p, size_t bytes, const char* what, cudaStream_t st)
+{
+    *p = nullptr;
+    if (bytes == 0) return RTS_OK;
+    if (ctx->used_bytes + (int64_t)bytes > ctx->budget_bytes)
+        return rts_fail(ctx, RTS_ERR_OVER_BUDGET,
+                        "%s: %zu bytes would exceed the HBM budget (%lld of %lld bytes in use)",
+                        what, bytes, (long long)ctx->used_bytes, (long long)ctx->budget_bytes);
+    if (!ctx->pool) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = ctx->device;
+        RTS_CUDA_TRY(ctx, cudaMemPoolCreate(&ctx->pool, &props));
+        uint64_t keep = UINT64_MAX;  // keep freed memory in the pool for the next problem
+        RTS_CUDA_TRY(ctx, cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ctx->pool, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return rts_fail(ctx, RTS_ERR_OUT_OF_MEMORY, "%s: pool allocation of %zu bytes failed: %s", what, bytes,
+                        cudaGetErrorString(e));
+    }
+    ctx->used_bytes += (int64_t)bytes;
+    return RTS_OK;
+}
+
+void rts_pfree(rts_ctx* ctx, void* p, size_t bytes, cudaStream_t st)
+{
+    if (!p) return;
+    cudaFreeAsync(p, st);
+    ctx->used_bytes -= (int64_t)bytes;
+}
+
 static void free_grid(rts_ctx* ctx)
 {
     const int64_t loc = ctx->local();
@@ -175,6 +211,17 @@ int rts_ctx_destroy(rts_ctx* ctx)
     free_grid(ctx);
     rts_dfree(ctx, ctx->d_resid, sizeof(unsigned long long) * (RTS_RESID_CAP + 1));
     rts_dfree(ctx, ctx->d_flag, sizeof(int) * 4);
+    for (int i = 0; i < RTS_STREAM_COUNT; ++i)
+        if (ctx->streams[i]) cudaStreamSynchronize(ctx->streams[i]);
+    if (ctx->serve_copy) {
+        cudaStreamSynchronize(ctx->serve_copy);
+        cudaStreamDestroy(ctx->serve_copy);
+    }
+    if (ctx->serve_admit) {
+        cudaStreamSynchronize(ctx->serve_admit);
+        cudaStreamDestroy(ctx->serve_admit);
+    }
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     for (int i = 0; i < RTS_STREAM_COUNT; ++i)
         if (ctx->streams[i]) cudaStreamDestroy(ctx->streams[i]);
     for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);

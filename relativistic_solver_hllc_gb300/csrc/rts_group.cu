@@ -93,19 +93,22 @@ struct rts_batch {
 
 namespace {
 
-void free_prob(rts_ctx* ctx, GProb* p)
+// frees are stream-ordered: after the work already queued on `st`
+void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
 {
     const size_t abytes = (size_t)(p->rows_pad * 2 * p->kpad * 2);
-    rts_dfree(ctx, p->wc, (size_t)(p->mpad * 2 * p->kpad * 2));
-    rts_dfree(ctx, p->cs, (size_t)(2 * p->mpad * 4));
-    rts_dfree(ctx, p->a[0], abytes);
-    rts_dfree(ctx, p->a[1], abytes);
-    rts_dfree(ctx, p->rs, (size_t)(2 * p->rows_pad * 4));
-    rts_dfree(ctx, p->B, (size_t)(p->rows * 4));
-    rts_dfree(ctx, p->lam, (size_t)(p->groups * 4));
-    rts_dfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4));
+    rts_pfree(ctx, p->wc, (size_t)(p->mpad * 2 * p->kpad * 2), st);
+    rts_pfree(ctx, p->cs, (size_t)(2 * p->mpad * 4), st);
+    rts_pfree(ctx, p->a[0], abytes, st);
+    rts_pfree(ctx, p->a[1], abytes, st);
+    rts_pfree(ctx, p->rs, (size_t)(2 * p->rows_pad * 4), st);
+    rts_pfree(ctx, p->B, (size_t)(p->rows * 4), st);
+    rts_pfree(ctx, p->lam, (size_t)(p->groups * 4), st);
+    rts_pfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4), st);
     delete p;
 }
+
+void free_prob(rts_ctx* ctx, GProb* p) { free_prob(ctx, p, ctx->streams[RTS_STREAM_SCATTERING_1]); }
 
 void drop_graph(rts_batch* b)
 {
@@ -114,14 +117,13 @@ void drop_graph(rts_batch* b)
     b->graph_steps = 0;
 }
 
-int ensure_scratch(rts_batch* b, size_t bytes)
+int ensure_scratch(rts_batch* b, size_t bytes, cudaStream_t st)
 {
     if (b->staging_bytes >= bytes) return RTS_OK;
-    cudaStreamSynchronize(b->ctx->streams[RTS_STREAM_SCATTERING_1]);
-    rts_dfree(b->ctx, b->staging, b->staging_bytes);
+    rts_pfree(b->ctx, b->staging, b->staging_bytes, st);
     b->staging = nullptr;
     b->staging_bytes = 0;
-    int rc = rts_dmalloc(b->ctx, &b->staging, bytes, "batch staging");
+    int rc = rts_pmalloc(b->ctx, &b->staging, bytes, "batch staging", st);
     if (rc == RTS_OK) b->staging_bytes = bytes;
     return rc;
 }
@@ -189,7 +191,8 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
 // Creates a problem: allocations, W (phase kernel on the given directions)
 // split into rows, tensor maps.  A rows, B and lambda are filled by the caller.
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev,
-                          int ldw, bool fp16, int flush, int bn_override, bool iterative, GProb** out)
+                          int ldw, bool fp16, int flush, int bn_override, bool iterative, GProb** out,
+                          cudaStream_t st)
 {
     rts_ctx* ctx = b->ctx;
     GProb* p = new GProb();
@@ -205,9 +208,10 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
                        &p->m_tiles);
     int rc;
     void* q;
+    if (!st) st = ctx->streams[RTS_STREAM_SCATTERING_1];
 #define GP_ALLOC(field, nbytes, name)                                 \
-    if ((rc = rts_dmalloc(ctx, &q, (nbytes), name)) != RTS_OK) {      \
-        free_prob(ctx, p);                                            \
+    if ((rc = rts_pmalloc(ctx, &q, (nbytes), name, st)) != RTS_OK) { \
+        free_prob(ctx, p, st);                                        \
         return rc;                                                    \
     }                                                                 \
     p->field = (decltype(p->field))q;                                 \
@@ -226,7 +230,6 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
         GP_ALLOC(S32, (size_t)(p->rows * p->Mout * 4), "FP32 scattering");
     }
 #undef GP_ALLOC
-    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
     if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
@@ -235,7 +238,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->kpad, G_BM);
     if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->kpad, G_BM);
     if (rc != RTS_OK) {
-        free_prob(ctx, p);
+        free_prob(ctx, p, st);
         return rc;
     }
     if (!p->a[1]) memcpy(p->maps[1], p->maps[0], 128);
@@ -280,8 +283,8 @@ void rts_group_batch_free(rts_batch* b)
     for (GProb* p : b->probs) free_prob(ctx, p);
     rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));
     rts_dfree(ctx, b->d_resid, b->resid_cap * sizeof(unsigned long long));
-    rts_dfree(ctx, b->staging, b->staging_bytes);
-    rts_dfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double));
+    rts_pfree(ctx, b->staging, b->staging_bytes, ctx->streams[RTS_STREAM_SCATTERING_1]);
+    rts_pfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double), ctx->streams[RTS_STREAM_SCATTERING_1]);
     for (int k = 0; k < 2; ++k) {
         if (b->h_pin[k]) cudaFreeHost(b->h_pin[k]);
         if (b->pin_ev[k]) cudaEventDestroy(b->pin_ev[k]);
@@ -578,29 +581,29 @@ int64_t rts_group_total_tiles(rts_batch* b)
 rts_ctx* rts_group_ctx(rts_batch* b) { return b->ctx; }
 size_t rts_group_count(rts_batch* b) { return b->probs.size(); }
 unsigned long long* rts_group_resid_slot(rts_batch* b, size_t index) { return b->d_resid + index; }
-int rts_group_scratch(rts_batch* b, size_t bytes, void** p)
+int rts_group_scratch(rts_batch* b, size_t bytes, void** p, cudaStream_t st)
 {
-    int rc = ensure_scratch(b, bytes);
+    int rc = ensure_scratch(b, bytes, st ? st : b->ctx->streams[RTS_STREAM_SCATTERING_1]);
     if (rc == RTS_OK) *p = b->staging;
     return rc;
 }
 
-int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t M, double** d_xyz, double** d_area)
+int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t M, double** d_xyz, double** d_area,
+                   cudaStream_t st)
 {
     rts_ctx* ctx = b->ctx;
+    if (!st) st = ctx->streams[RTS_STREAM_SCATTERING_1];
     const size_t need = (size_t)(4 * M);
     if (b->dirs_cap < need) {
-        cudaStreamSynchronize(ctx->streams[RTS_STREAM_SCATTERING_1]);
-        rts_dfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double));
+        rts_pfree(ctx, b->d_dirs, b->dirs_cap * sizeof(double), st);
         b->d_dirs = nullptr;
         b->dirs_cap = 0;
         void* q;
-        int rc = rts_dmalloc(ctx, &q, need * sizeof(double), "batch directions");
+        int rc = rts_pmalloc(ctx, &q, need * sizeof(double), "batch directions", st);
         if (rc != RTS_OK) return rc;
         b->d_dirs = (double*)q;
         b->dirs_cap = need;
     }
-    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_dirs, xyz, (size_t)(3 * M) * 8, cudaMemcpyHostToDevice, st));
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_dirs + 3 * M, area, (size_t)M * 8, cudaMemcpyHostToDevice, st));
     *d_xyz = b->d_dirs;
@@ -608,13 +611,16 @@ int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t 
     return RTS_OK;
 }
 
-int rts_group_remove(rts_batch* b, int64_t id)
+int rts_group_remove(rts_batch* b, int64_t id) { return rts_group_remove_on(b, id, nullptr); }
+
+// The problem's buffers are freed in the order of `st` (the scattering stream
+// when null): after every launch or copy already queued there.
+int rts_group_remove_on(rts_batch* b, int64_t id, cudaStream_t st)
 {
     size_t idx = 0;
     GProb* p = rts_group_find(b, id, &idx);
     RTS_REQUIRE(b->ctx, p, RTS_ERR_INVALID_ARGUMENT, "no problem with id %lld in the batch", (long long)id);
-    cudaStreamSynchronize(b->ctx->streams[RTS_STREAM_SCATTERING_1]);
-    free_prob(b->ctx, p);
+    free_prob(b->ctx, p, st ? st : b->ctx->streams[RTS_STREAM_SCATTERING_1]);
     b->probs.erase(b->probs.begin() + (long)idx);
     b->dirty = true;
     drop_graph(b);

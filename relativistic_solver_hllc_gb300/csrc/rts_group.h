@@ -40,11 +40,15 @@ void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override
 int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative);
 int rts_group_batch_new(rts_ctx* ctx, rts_batch** out);
 void rts_group_batch_free(rts_batch* b);
+// buffers allocated and initialised on st (null: the scattering stream)
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev, int ldw,
-                          bool fp16, int flush, int bn_override, bool iterative, GProb** out);
+                          bool fp16, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr);
 int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
 GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
 int rts_group_remove(rts_batch* b, int64_t id);
+int rts_group_remove_on(rts_batch* b, int64_t id, cudaStream_t st);
+int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* ibar, const float* B,
+                     const double* lambda, cudaStream_t st, bool sync, int64_t* id);
 int rts_group_step(rts_batch* b, int relax, cudaStream_t st);
 // Builds and uploads the device table now (a later step of an unchanged batch
 // then queues its launch without a host synchronisation).
@@ -58,9 +62,10 @@ int rts_group_replay(rts_batch* b);
 int64_t rts_group_total_tiles(rts_batch* b);
 size_t rts_group_count(rts_batch* b);
 unsigned long long* rts_group_resid_slot(rts_batch* b, size_t index);
-int rts_group_scratch(rts_batch* b, size_t bytes, void** p);
+// st: stream the scratch and direction buffers are used on (null: the scattering stream)
+int rts_group_scratch(rts_batch* b, size_t bytes, void** p, cudaStream_t st = nullptr);
 int rts_group_dirs(rts_batch* b, const double* xyz, const double* area, int64_t M, double** d_xyz,
-                   double** d_area);
+                   double** d_area, cudaStream_t st = nullptr);
 rts_ctx* rts_group_ctx(rts_batch* b);
 // Forces the device table to be rebuilt before the next launch (after the
 // caller changed cur / S64 / use_B of a problem) and drops a captured graph.

@@ -100,6 +100,9 @@ struct rts_ctx {
     unsigned long long* d_resid = nullptr;
     unsigned long long* resid_target = nullptr;  // slot the next kernels reduce into
     int* d_flag = nullptr;       // device-side error flag of bounded waits
+    cudaMemPool_t pool = nullptr;  // stream-ordered pool of the batched problems' buffers (created on first use)
+    cudaStream_t serve_copy = nullptr;  // read-backs of finished serving requests
+    cudaStream_t serve_admit = nullptr;  // set-up of admitted serving requests (lowest priority)
 
     // source iteration
     int solve_precision = -1;
@@ -133,6 +136,11 @@ void rts_timing_end(rts_ctx* ctx, cudaStream_t st);
 // Device allocation accounted against the context's HBM budget.
 int rts_dmalloc(rts_ctx* ctx, void** p, size_t bytes, const char* what);
 void rts_dfree(rts_ctx* ctx, void* p, size_t bytes);
+// Stream-ordered allocation from the context's pool (no device-wide
+// synchronisation on either call; freed memory stays cached for reuse).
+// Counted against the same HBM budget as rts_dmalloc.
+int rts_pmalloc(rts_ctx* ctx, void** p, size_t bytes, const char* what, cudaStream_t st);
+void rts_pfree(rts_ctx* ctx, void* p, size_t bytes, cudaStream_t st);
 
 // Kernel launchers (defined in the .cu files).
 int rts_launch_scatter_fp64(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaStream_t st,

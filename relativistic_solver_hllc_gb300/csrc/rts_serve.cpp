@@ -4,7 +4,10 @@
 // arrive over time.  One host thread drives one device batch:
 //   * admission: arrived requests join the batch in arrival order as long as
 //     the context's device bytes plus the request's resident footprint stay
-//     under the HBM cap; a request larger than the cap is rejected;
+//     under the HBM cap; a request larger than the cap is rejected.  Its
+//     set-up (W, copies, split) is queued on a low-priority stream of its own
+//     and overlaps the running steps; the request takes part in steps once
+//     that set-up has finished;
 //   * every step advances resident requests by one source iteration in one
 //     grouped tcgen05 launch, so requests that arrive while others run share
 //     the device from their first step on.  Which ones (RTS_TUNE_SERVE_POLICY):
@@ -15,8 +18,12 @@
 //     keeps launches short -- a request's step is cut into pieces of tiles
 //     when it does not fit, so a large step never holds back an urgent small
 //     request for long; or all of them, one whole step each;
-//   * a request that has run its iterations is read back (S, FP32) and
-//     leaves the batch, freeing its memory for waiting requests.
+//   * a request that has run its iterations is read back (S, FP32) on a copy
+//     stream and leaves the batch, freeing its memory for waiting requests.
+// The host keeps up to G_INFLIGHT steps queued ahead of the device (each with
+// an event), so set-up, retirement and scheduling overlap the running step;
+// problem buffers come from a stream-ordered pool, so admitting or retiring a
+// request never synchronises the device.
 // Latency = completion time - arrival time (host wall clock).  Waits on the
 // device are bounded; nothing here blocks forever.
 //
@@ -50,6 +57,8 @@ double percentile(std::vector<double> v, double q)
     return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
 }
 
+constexpr int G_INFLIGHT = 2;  // steps queued ahead of the device
+
 struct Active {
     int64_t req = 0;
     int64_t id = 0;
@@ -60,7 +69,30 @@ struct Active {
     int waited = 0;       // consecutive steps left out
     double deadline = 0;  // arrival + 2 x estimated isolated solve time (s)
     int64_t pos = 0;      // next tile of the current step (a step may span launches)
+    int state = 0;        // -1 set-up queued, 0 running, 1 last step queued, 2 read-back queued
+    cudaEvent_t ready = nullptr;   // set-up done (state -1)
+    cudaEvent_t copied = nullptr;  // read-back done (state 2)
 };
+
+struct Queued {  // a launched step: its completion event and the requests it finishes
+    cudaEvent_t done = nullptr;
+    std::vector<int64_t> finishing;  // batch ids
+};
+
+// Polls an event until it completes or `timeout_us` passes (< 0: no limit).
+int wait_event(rts_ctx* ctx, cudaEvent_t ev, int64_t timeout_us)
+{
+    const auto t0 = clock_type::now();
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess) return RTS_OK;
+        if (e != cudaErrorNotReady) return rts_fail(ctx, RTS_ERR_CUDA, "serving: %s", cudaGetErrorString(e));
+        if (timeout_us >= 0 && seconds_since(t0) * 1e6 > (double)timeout_us)
+            return rts_fail(ctx, RTS_ERR_TIMEOUT, "serving: a step did not finish within %lld us",
+                            (long long)timeout_us);
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
 
 // Solve time of a request alone: per step a fixed launch and host overhead
 // plus its tiles in waves over the SMs, each tile taking about 1 us per
@@ -90,9 +122,32 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
     rts_batch* batch = nullptr;
     int rc = rts_batch_create(ctx, &batch);
     if (rc != RTS_OK) return rc;
+    if (!ctx->serve_copy && cudaStreamCreateWithFlags(&ctx->serve_copy, cudaStreamNonBlocking) != cudaSuccess) {
+        rts_batch_destroy(batch);
+        return rts_fail(ctx, RTS_ERR_CUDA, "serving: cannot create the copy stream");
+    }
+    if (!ctx->serve_admit) {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (cudaStreamCreateWithPriority(&ctx->serve_admit, cudaStreamNonBlocking, least) != cudaSuccess) {
+            rts_batch_destroy(batch);
+            return rts_fail(ctx, RTS_ERR_CUDA, "serving: cannot create the set-up stream");
+        }
+    }
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    std::vector<cudaEvent_t> events;  // free list
+    auto take_event = [&](cudaEvent_t* ev) {
+        if (!events.empty()) {
+            *ev = events.back();
+            events.pop_back();
+            return cudaSuccess;
+        }
+        return cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    };
 
     std::deque<int64_t> waiting;
     std::vector<Active> active;
+    std::deque<Queued> queued;
     std::vector<double> lat;
     int64_t next = 0, done = 0, rejected = 0, steps = 0, peak = ctx->used_bytes, max_active = 0;
     double work = 0.0;  // cell-direction-iterations completed
@@ -100,7 +155,77 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
     const int64_t base_bytes = ctx->used_bytes;
     const auto t0 = clock_type::now();
 
+    auto fail = [&](int code) {
+        cudaStreamSynchronize(st);
+        cudaStreamSynchronize(ctx->serve_copy);
+        for (Queued& q : queued) events.push_back(q.done);
+        cudaStreamSynchronize(ctx->serve_admit);
+        for (Active& a : active) {
+            if (a.copied) events.push_back(a.copied);
+            if (a.ready) events.push_back(a.ready);
+        }
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        rts_batch_destroy(batch);
+        return code;
+    };
+    // the oldest queued step finished: queue the read-back of every request it completed
+    auto finish_step = [&]() -> int {
+        Queued& q = queued.front();
+        for (int64_t id : q.finishing) {
+            for (Active& a : active) {
+                if (a.id != id) continue;
+                const rts_request& rq = reqs[a.req];
+                GProb* p = rts_group_find(batch, id, nullptr);
+                if (rq.S_out && p && p->S32 &&
+                    cudaMemcpyAsync(rq.S_out, p->S32, (size_t)(p->rows * p->Mout) * 4, cudaMemcpyDeviceToHost,
+                                    ctx->serve_copy) != cudaSuccess)
+                    return rts_fail(ctx, RTS_ERR_CUDA, "serving: read-back failed");
+                if (take_event(&a.copied) != cudaSuccess || cudaEventRecord(a.copied, ctx->serve_copy) != cudaSuccess)
+                    return rts_fail(ctx, RTS_ERR_CUDA, "serving: event record failed");
+                a.state = 2;
+            }
+        }
+        events.push_back(q.done);
+        queued.pop_front();
+        return RTS_OK;
+    };
+    // requests whose read-back has landed leave the batch
+    auto retire = [&]() -> int {
+        for (size_t i = 0; i < active.size();) {
+            Active& a = active[i];
+            if (a.state != 2 || cudaEventQuery(a.copied) != cudaSuccess) {
+                ++i;
+                continue;
+            }
+            const double tr = seconds_since(t0);
+            const rts_request& q = reqs[a.req];
+            const int r2 = rts_group_remove_on(batch, a.id, ctx->serve_copy);  // freed after the read-back
+            retire_s += seconds_since(t0) - tr;
+            if (r2 != RTS_OK) return r2;
+            const double l = (seconds_since(t0) - q.arrival_s) * 1e3;
+            if (latency_ms) latency_ms[a.req] = l;
+            lat.push_back(l);
+            work += (double)q.desc.N * (double)q.desc.groups * (double)q.desc.M * (double)q.iterations;
+            ++done;
+            events.push_back(a.copied);
+            active[i] = active.back();
+            active.pop_back();
+        }
+        return RTS_OK;
+    };
+
     while (done + rejected < n) {
+        // completed steps and read-backs first: they free memory and slots
+        while (!queued.empty() && cudaEventQuery(queued.front().done) == cudaSuccess)
+            if ((rc = finish_step()) != RTS_OK) return fail(rc);
+        if ((rc = retire()) != RTS_OK) return fail(rc);
+        for (Active& a : active)
+            if (a.state == -1 && cudaEventQuery(a.ready) == cudaSuccess) {
+                a.state = 0;
+                events.push_back(a.ready);
+                a.ready = nullptr;
+            }
+
         const double now = seconds_since(t0);
         while (next < n && reqs[next].arrival_s <= now) waiting.push_back(next++);
         // admission in arrival order while the HBM cap allows
@@ -119,7 +244,10 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             if (ctx->used_bytes + fp + scratch > hbm_cap && !active.empty()) break;
             int64_t id = 0;
             const double ta = seconds_since(t0);
-            rc = rts_batch_add(batch, &d, reqs[r].ibar, reqs[r].B, reqs[r].lambda, &id);
+            rc = rts_batch_add_on(batch, &d, reqs[r].ibar, reqs[r].B, reqs[r].lambda, ctx->serve_admit, false, &id);
+            cudaEvent_t ready = nullptr;
+            if (rc == RTS_OK && (take_event(&ready) != cudaSuccess || cudaEventRecord(ready, ctx->serve_admit) != cudaSuccess))
+                rc = rts_fail(ctx, RTS_ERR_CUDA, "serving: event record failed");
             admit_s += seconds_since(t0) - ta;
             if (rc == RTS_ERR_OVER_BUDGET || rc == RTS_ERR_OUT_OF_MEMORY) {
                 if (active.empty()) {  // nothing will free memory: reject
@@ -129,31 +257,53 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
                 }
                 break;
             }
-            if (rc != RTS_OK) {
-                rts_batch_destroy(batch);
-                return rc;
-            }
+            if (rc != RTS_OK) return fail(rc);
             const int64_t tiles = rts_group_problem_tiles(batch, id);
-            active.push_back(Active{r, id, reqs[r].iterations, fp, tiles,
-                                    (double)d.N * (double)d.groups * (double)d.M * (double)d.M, 0,
-                                    reqs[r].arrival_s + 0.01 * ctx->serve_slack *
-                                                            isolated_estimate(tiles, d.M, reqs[r].iterations,
-                                                                              ctx->num_sms)});
+            Active a;
+            a.req = r;
+            a.id = id;
+            a.remaining = reqs[r].iterations;
+            a.bytes = fp;
+            a.tiles = tiles;
+            a.step_work = (double)d.N * (double)d.groups * (double)d.M * (double)d.M;
+            a.deadline = reqs[r].arrival_s +
+                         0.01 * ctx->serve_slack * isolated_estimate(tiles, d.M, reqs[r].iterations, ctx->num_sms);
+            a.state = -1;
+            a.ready = ready;
+            active.push_back(a);
             waiting.pop_front();
             peak = std::max(peak, ctx->used_bytes);
         }
         max_active = std::max<int64_t>(max_active, (int64_t)active.size());
-        if (active.empty()) {
+
+        // requests with iterations still to launch
+        std::vector<size_t> order;
+        for (size_t i = 0; i < active.size(); ++i)
+            if (active[i].state == 0) order.push_back(i);
+        if (order.empty() || (int)queued.size() >= G_INFLIGHT) {
+            // nothing to launch now: wait for the device (a step or a read-back)
+            if (!queued.empty()) {
+                const double tw = seconds_since(t0);
+                rc = wait_event(ctx, queued.front().done, step_timeout_us);
+                step_s += seconds_since(t0) - tw;
+                if (rc != RTS_OK) return fail(rc);
+                continue;
+            }
+            bool copying = false;
+            for (const Active& a : active) copying |= a.state == 2 || a.state == -1;
+            if (copying) {
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                continue;
+            }
             if (next < n) {
                 const double wait = reqs[next].arrival_s - seconds_since(t0);
                 if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
                 continue;
             }
-            break;  // only rejected requests were left
+            if (active.empty()) break;  // only rejected requests were left
+            continue;
         }
         // the pieces this launch runs: (request, first tile, tiles)
-        std::vector<size_t> order(active.size());
-        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
         std::vector<int64_t> take(active.size(), 0);
         if (ctx->serve_policy != 0) {
             auto key = [&](size_t i) {
@@ -169,10 +319,10 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
                 left -= take[i];
             }
         } else {
-            for (size_t i = 0; i < active.size(); ++i) take[i] = active[i].tiles - active[i].pos;
+            for (size_t i : order) take[i] = active[i].tiles - active[i].pos;
         }
         std::vector<int64_t> ids, first, count;
-        for (size_t i = 0; i < active.size(); ++i) {
+        for (size_t i : order) {
             if (take[i] > 0) {
                 ids.push_back(active[i].id);
                 first.push_back(active[i].pos);
@@ -183,47 +333,34 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
             }
         }
         const double ts = seconds_since(t0);
-        rc = rts_group_step_pieces(batch, 1, ids.data(), first.data(), count.data(), (int)ids.size(),
-                                   ctx->streams[RTS_STREAM_SCATTERING_1]);
-        if (rc == RTS_OK) rc = rts_batch_sync(batch, step_timeout_us);
+        rc = rts_group_step_pieces(batch, 1, ids.data(), first.data(), count.data(), (int)ids.size(), st);
+        Queued q;
+        if (rc == RTS_OK && (take_event(&q.done) != cudaSuccess || cudaEventRecord(q.done, st) != cudaSuccess))
+            rc = rts_fail(ctx, RTS_ERR_CUDA, "serving: event record failed");
         step_s += seconds_since(t0) - ts;
-        if (rc != RTS_OK) {
-            rts_batch_destroy(batch);
-            return rc;
-        }
-        for (size_t i = 0; i < active.size(); ++i) {
-            active[i].pos += take[i];
-            if (take[i] > 0 && active[i].pos == active[i].tiles) {  // the step is complete
-                active[i].pos = 0;
-                active[i].remaining--;
-            }
-        }
-        ++steps;
-        // completions
-        for (size_t i = 0; i < active.size();) {
+        if (rc != RTS_OK) return fail(rc);
+        for (size_t i : order) {
             Active& a = active[i];
-            if (a.remaining > 0) {
-                ++i;
-                continue;
+            a.pos += take[i];
+            if (take[i] > 0 && a.pos == a.tiles) {  // the step is complete
+                a.pos = 0;
+                if (--a.remaining == 0) {
+                    a.state = 1;
+                    q.finishing.push_back(a.id);
+                }
             }
-            const rts_request& q = reqs[a.req];
-            const double tr = seconds_since(t0);
-            rc = rts_batch_read(batch, a.id, q.S_out, nullptr);
-            if (rc == RTS_OK) rc = rts_batch_remove(batch, a.id);
-            retire_s += seconds_since(t0) - tr;
-            if (rc != RTS_OK) {
-                rts_batch_destroy(batch);
-                return rc;
-            }
-            const double l = (seconds_since(t0) - q.arrival_s) * 1e3;
-            if (latency_ms) latency_ms[a.req] = l;
-            lat.push_back(l);
-            work += (double)q.desc.N * (double)q.desc.groups * (double)q.desc.M * (double)q.iterations;
-            ++done;
-            active[i] = active.back();
-            active.pop_back();
         }
+        queued.push_back(q);
+        ++steps;
     }
+    // a bounded wait reported on the device invalidates the results
+    int flag = 0;
+    if (cudaStreamSynchronize(ctx->serve_copy) != cudaSuccess || cudaStreamSynchronize(ctx->serve_admit) != cudaSuccess ||
+        cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(rts_fail(ctx, RTS_ERR_CUDA, "serving: final synchronisation failed"));
+    if (flag) return fail(rts_fail(ctx, RTS_ERR_DEVICE_WAIT, "serving: the batched kernel reported device flag %d", flag));
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    events.clear();
     const double makespan = seconds_since(t0);
     rts_batch_destroy(batch);
     stats->completed = done;
