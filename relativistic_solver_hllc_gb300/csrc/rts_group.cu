@@ -41,18 +41,21 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn(rts_ctx* ctx)
     return fn;
 }
 
-// 2-D map over interleaved split rows [rows][2*kpad] (16-bit): box of 64
-// halves x box_rows, 128-byte swizzle.
-int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t kpad, int box_rows)
+// 2-D map over interleaved split rows [rows][2*kpad] (16-bit): box of
+// box_cols halves x box_rows; the MMA operands use 64 x rows with a 128-byte
+// swizzle, the relaxation 8 x 32 unswizzled (16 bytes of each of 32 rows).
+int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t kpad, int box_rows, int box_cols = 64,
+             bool swizzle = true)
 {
     auto enc = encode_fn(ctx);
     if (!enc) return RTS_ERR_CUDA;
     cuuint64_t dims[2] = {(cuuint64_t)(2 * kpad), (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)(2 * kpad * 2)};
-    cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1u, 1u};
     CUresult r = enc(reinterpret_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base),
-                     dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return rts_fail(ctx, RTS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for %lld x %lld", (int)r,
@@ -237,11 +240,14 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->kpad, p->bn);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->kpad, G_BM);
     if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->kpad, G_BM);
+    if (rc == RTS_OK) rc = make_map(ctx, p->rmaps[0], p->a[0], p->rows_pad, p->kpad, 32, 8, false);
+    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->rmaps[1], p->a[1], p->rows_pad, p->kpad, 32, 8, false);
     if (rc != RTS_OK) {
         free_prob(ctx, p, st);
         return rc;
     }
     if (!p->a[1]) memcpy(p->maps[1], p->maps[0], 128);
+    if (!p->a[1]) memcpy(p->rmaps[1], p->rmaps[0], 128);
     *out = p;
     return RTS_OK;
 }
@@ -306,6 +312,8 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     memcpy(&g.mapA[0], p->maps[0], 128);
     memcpy(&g.mapA[1], p->maps[1], 128);
     memcpy(&g.mapW, p->maps[2], 128);
+    memcpy(&g.mapR[0], p->rmaps[0], 128);
+    memcpy(&g.mapR[1], p->rmaps[1], 128);
     g.N = p->N;
     g.ldS = p->ldS > 0 ? p->ldS : p->N;
     g.rows = p->rows;

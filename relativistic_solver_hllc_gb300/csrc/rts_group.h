@@ -33,6 +33,7 @@ struct GProb {
     int slot = -1;           // index of the problem's residual in the last launched table
     size_t bytes = 0;
     alignas(64) unsigned char maps[3][128];
+    alignas(64) unsigned char rmaps[2][128];  // relaxation boxes of a[0], a[1]
 };
 
 void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override, int* bn, int* n_tiles, int64_t* kpad,

@@ -50,8 +50,8 @@ constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
 constexpr int G_CTAS_PER_SM = 1;
 constexpr uint32_t G_TMEM_COLS = 512;
 constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
-constexpr int G_BAR_BYTES = 256;
-constexpr int G_REL_BUF = 2 * 32 * 32;  // per epilogue warp: 2 buffers x 32 rows x (16 B hi + 16 B lo)
+constexpr int G_BAR_BYTES = 512;  // ring, accumulator and relaxation barriers, TMEM address
+constexpr int G_REL_BUF = 2 * 1024;  // per epilogue warp: 2 buffers x (32 rows x 16 B hi, then 32 rows x 16 B lo)
 constexpr size_t G_REL_OFF = (size_t)G_STAGES * G_STAGE_BYTES + G_BAR_BYTES;
 constexpr size_t G_SMEM = G_REL_OFF + (size_t)G_EPI_WARPS * G_REL_BUF + 1024;
 static_assert(G_SMEM <= 227 * 1024, "shared memory per CTA");
@@ -59,6 +59,7 @@ static_assert(G_SMEM <= 227 * 1024, "shared memory per CTA");
 struct GroupProblem {  // aligned as its CUtensorMap members
     CUtensorMap mapA[2];  // split Ibar, ping-pong buffers
     CUtensorMap mapW;     // split W^T
+    CUtensorMap mapR[2];  // split Ibar in relaxation boxes (8 columns x 32 rows), ping-pong buffers
     int64_t N;            // cells per group
     int64_t ldS;          // row pitch of S32 / S64 in cells (>= N; N unless the output is a cell range of a wider S)
     int64_t rows;         // groups * N
@@ -128,13 +129,15 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G_STAGES * G_STAGE_BYTES);  // G_BAR_BYTES
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * G_STAGES + 4);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 48);
     const uint32_t smem_base = smem_u32(smem);
     const uint32_t bar_base = smem_u32(bars);
     auto full_bar = [&](int s) { return bar_base + 8u * s; };
     auto empty_bar = [&](int s) { return bar_base + 8u * (G_STAGES + s); };
     auto acc_full_bar = [&](int a) { return bar_base + 8u * (2 * G_STAGES + a); };
     auto acc_empty_bar = [&](int a) { return bar_base + 8u * (2 * G_STAGES + 2 + a); };
+    // relaxation row buffers: barrier of buffer b of epilogue warp w
+    auto rel_bar = [&](int w, uint32_t b) { return bar_base + 8u * (16 + 2 * w + (int)b); };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -145,6 +148,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
         for (int a = 0; a < 2; ++a) {
             mbar_init(acc_full_bar(a), 1);
             mbar_init(acc_empty_bar(a), G_EPI_WARPS);
+        }
+        for (int w = 0; w < G_EPI_WARPS; ++w) {
+            mbar_init(rel_bar(w, 0), 1);
+            mbar_init(rel_bar(w, 1), 1);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -245,6 +252,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
         const int q = warp & 3;                    // TMEM lane quarter
         const int cs = (warp - G_EPI_WARP0) >> 2;  // 64-column slice of the tile
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        const int ew = warp - G_EPI_WARP0;
+        uint8_t* rbuf = smem + G_REL_OFF + (size_t)ew * G_REL_BUF;
+        const uint32_t rbuf_s = smem_u32(rbuf);
+        uint32_t rel_issued = 0, rel_used = 0;  // relaxation row blocks fetched / consumed by this warp
         uint32_t gch = 0;
         bool ok = live;
         for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
@@ -353,31 +364,29 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             const int kbase = n_tile * bn + 64 * cs;
-            // The relaxation's split rows go through a double buffer per warp in
-            // shared memory, 8 columns (hi 16 B + lo 16 B per row) per step:
-            // the next step's rows are fetched with cp.async while this step
-            // computes, and rows are read and written two lanes per row (rows
-            // are 4*kpad bytes apart: one lane per row would touch 32 lines
-            // per instruction).
+            // The relaxation's split rows of each block of 8 columns (16 B hi and
+            // 16 B lo of each of the warp's 32 rows) move by TMA: a 2-D box load
+            // into one of two shared-memory buffers per warp, one block ahead,
+            // and after the update a box store back into the other ping-pong
+            // buffer.  A buffer is refilled only once the store that read it
+            // has finished reading (rows 4*kpad bytes apart would otherwise cost
+            // a line per lane on every access).
             const bool want_rel = relax && S64 == nullptr;  // relax implies Mout == M <= kpad
-            const int64_t rstride = 4 * (int64_t)kpad;       // bytes per split row
-            const int64_t row0 = (int64_t)m_tile * G_BM + q * 32;
-            const uint8_t* __restrict__ abase = reinterpret_cast<const uint8_t*>(P.a[P.cur]) + row0 * rstride;
-            uint8_t* __restrict__ nbase = reinterpret_cast<uint8_t*>(P.a[P.cur ^ 1]) + row0 * rstride;
-            uint8_t* rbuf = smem + G_REL_OFF + (size_t)(warp - G_EPI_WARP0) * G_REL_BUF;
-            const uint32_t rbuf_s = smem_u32(rbuf);
-            // row rr keeps hi at rr*32 + 16*(rr>>2 & 1) and lo in the other half
-            auto slot = [](int rr, int part) { return rr * 32 + ((part ^ ((rr >> 2) & 1)) << 4); };
-            auto fetch = [&](int e0, int b) {  // rows 16i + lane/2, part lane%2 (0 hi, 1 lo)
+            const int row0 = m_tile * G_BM + q * 32;
+            const void* map_in = &P.mapR[P.cur];
+            const void* map_out = &P.mapR[P.cur ^ 1];
+            auto fetch = [&](int e0) {
                 const int k0 = kbase + e0;
-                if (!want_rel || k0 >= Mout) return;
-                const int64_t boff = (int64_t)(k0 >> 5) * 128 + (k0 & 31) * 2;
-#pragma unroll
-                for (int i = 0; i < 2; ++i) {
-                    const int rr = 16 * i + (lane >> 1), part = lane & 1;
-                    cp_async16(rbuf_s + (uint32_t)(b * (G_REL_BUF / 2) + slot(rr, part)),
-                               abase + rr * rstride + boff + part * 64);
+                if (!want_rel || k0 >= Mout || e0 >= ncols) return;
+                if (lane == 0) {
+                    const uint32_t b = rel_issued & 1u, dst = rbuf_s + b * 1024u;
+                    const int x = (k0 >> 5) * 64 + (k0 & 31);
+                    bulk_wait_read0();  // the store that last read this buffer
+                    mbar_expect_tx(rel_bar(ew, b), 1024);
+                    tma_load_2d(dst, map_in, x, row0, rel_bar(ew, b));
+                    tma_load_2d(dst + 512u, map_in, x + 32, row0, rel_bar(ew, b));
                 }
+                ++rel_issued;
             };
             float rmax = 0.0f;
             bool overflow = false;
@@ -396,16 +405,14 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             };
             float old_next[8];
             load_old(0, old_next);
-            fetch(0, 0);
-            cp_async_commit();
+            fetch(0);
 #pragma unroll 1
-            for (int e0 = 0, st = 0; e0 < ncols; e0 += 8, ++st) {
+            for (int e0 = 0; e0 < ncols; e0 += 8) {
                 const int k0 = kbase + e0;
                 const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
                 const bool live_k = in_row && nk > 0;
                 const bool rel = want_rel && nk > 0;  // same for all lanes
-                if (e0 + 8 < ncols) fetch(e0 + 8, (st + 1) & 1);
-                cp_async_commit();
+                if (e0 + 8 < ncols) fetch(e0 + 8);
                 float old[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) old[j] = old_next[j];
@@ -421,14 +428,11 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     for (int j = 0; j < 8; ++j) cin[j] = 1.0f;
                 }
                 float v[8];
-                cp_async_wait1();
-                __syncwarp();
                 tmem_ld8(last_acc + (uint32_t)e0, v);
-                uint8_t* rb = rbuf + (st & 1) * (G_REL_BUF / 2);
-                if (live_k) {
-                    float snew[8];
+                float snew[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
+                for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
+                if (live_k) {
                     if (S64) {
                         double* dp = S64 + (int64_t)k0 * ld;
 #pragma unroll
@@ -442,30 +446,38 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                                 *sp = snew[j];
                                 rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
                             }
-                        if (rel) {
-                            uint4* hp = reinterpret_cast<uint4*>(rb + slot(lane, 0));
-                            uint4* lp = reinterpret_cast<uint4*>(rb + slot(lane, 1));
-                            if (fp16)
-                                overflow |= relax8<true>(hp, lp, snew, hrsc, nk);
-                            else
-                                relax8<false>(hp, lp, snew, hrsc, nk);
-                        }
                     }
                 }
                 if (rel) {
-                    // rows outside the problem go back unchanged
+                    // this block's rows: wait for the load, relax this lane's
+                    // row in place (rows outside the problem stay unchanged),
+                    // store the box into the other ping-pong buffer
+                    const uint32_t b = rel_used & 1u;
+                    const bool got = mbar_wait(rel_bar(ew, b), (rel_used >> 1) & 1u, flag, FLAG_WAIT_EPILOGUE);
+                    ++rel_used;
+                    if (!__all_sync(0xffffffffu, got)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* rb = rbuf + b * 1024u;
+                    if (live_k) {
+                        uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
+                        uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
+                        if (fp16)
+                            overflow |= relax8<true>(hp, lp, snew, hrsc, nk);
+                        else
+                            relax8<false>(hp, lp, snew, hrsc, nk);
+                    }
+                    fence_proxy_async_smem();
                     __syncwarp();
-                    const int64_t boff = (int64_t)(k0 >> 5) * 128 + (k0 & 31) * 2;
-#pragma unroll
-                    for (int i = 0; i < 2; ++i) {
-                        const int rr = 16 * i + (lane >> 1), part = lane & 1;
-                        *reinterpret_cast<uint4*>(nbase + rr * rstride + boff + part * 64) =
-                            *reinterpret_cast<const uint4*>(rb + slot(rr, part));
+                    if (lane == 0) {
+                        const int x = (k0 >> 5) * 64 + (k0 & 31);
+                        tma_store_2d(map_out, x, row0, rbuf_s + b * 1024u);
+                        tma_store_2d(map_out, x + 32, row0, rbuf_s + b * 1024u + 512u);
+                        bulk_commit();
                     }
                 }
-                __syncwarp();  // this buffer is refilled two steps on
             }
-            cp_async_wait0();
             release_last();
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
@@ -475,6 +487,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     atomicMax(P.resid, (unsigned long long)__double_as_longlong((double)rmax));
             }
         }
+        if (lane == 0) bulk_wait0();  // the relaxation's stores are complete before the CTA exits
     }
     tc_fence_before();
     __syncthreads();
