@@ -61,7 +61,9 @@ typedef enum rts_phase {
 typedef enum rts_precision {
     RTS_PREC_FP64 = 0,   /* FP64 CUDA cores; matches the CPU integral to 1e-12 relative */
     RTS_PREC_BF16X3 = 1, /* tcgen05 tensor cores, split BF16 hi/lo, three products, FP32 accumulate */
-    RTS_PREC_FP16X3 = 2  /* tcgen05 tensor cores, scaled split FP16 hi/lo, three products, FP32 accumulate */
+    RTS_PREC_FP16X3 = 2, /* tcgen05 tensor cores, scaled split FP16 hi/lo, three products, FP32 accumulate */
+    RTS_PREC_TF32X3 = 3  /* tcgen05 tensor cores (kind::tf32), split TF32 hi/lo, three products, FP32
+                            accumulate: no scaling, FP32 range, half the FP16 path's tensor rate */
 } rts_precision;
 
 typedef struct rts_ctx rts_ctx;

@@ -11,6 +11,7 @@ from ._native import (  # noqa: F401
     PHASE_THOMSON,
     PREC_BF16X3,
     PREC_FP16X3,
+    PREC_TF32X3,
     PREC_FP64,
     PRECISIONS,
     STREAM_PARAMS,

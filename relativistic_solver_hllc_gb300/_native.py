@@ -47,8 +47,9 @@ PHASE_CUSTOM = 2
 PREC_FP64 = 0
 PREC_BF16X3 = 1
 PREC_FP16X3 = 2
+PREC_TF32X3 = 3
 
-PRECISIONS = {"fp64": PREC_FP64, "bf16x3": PREC_BF16X3, "fp16x3": PREC_FP16X3}
+PRECISIONS = {"fp64": PREC_FP64, "bf16x3": PREC_BF16X3, "fp16x3": PREC_FP16X3, "tf32x3": PREC_TF32X3}
 
 
 class RtsError(RuntimeError):

@@ -25,7 +25,9 @@ int check_desc(rts_ctx* ctx, const rts_problem_desc* d)
                 "phase must be RTS_PHASE_THOMSON or RTS_PHASE_HG");
     RTS_REQUIRE(ctx, d->phase != RTS_PHASE_HG || (d->g > -1.0 && d->g < 1.0), RTS_ERR_INVALID_ARGUMENT,
                 "HG asymmetry %g outside (-1, 1)", d->g);
-    RTS_REQUIRE(ctx, d->precision == RTS_PREC_FP16X3 || d->precision == RTS_PREC_BF16X3, RTS_ERR_INVALID_ARGUMENT,
+    RTS_REQUIRE(ctx, d->precision == RTS_PREC_FP16X3 || d->precision == RTS_PREC_BF16X3 ||
+                         d->precision == RTS_PREC_TF32X3,
+                RTS_ERR_INVALID_ARGUMENT,
                 "batched problems run the tensor-core precisions only");
     RTS_REQUIRE(ctx, d->flush >= 0 && d->flush <= 2, RTS_ERR_INVALID_ARGUMENT, "flush %d outside [0,2]", d->flush);
     RTS_REQUIRE(ctx, d->bn == 0 || (d->bn % 16 == 0 && d->bn >= 16 && d->bn <= 256), RTS_ERR_INVALID_ARGUMENT,
@@ -40,7 +42,7 @@ extern "C" {
 int rts_problem_footprint(const rts_problem_desc* desc, int64_t* bytes)
 {
     if (!desc || !bytes || desc->N <= 0 || desc->M <= 0 || desc->groups <= 0) return RTS_ERR_INVALID_ARGUMENT;
-    *bytes = rts_group_footprint(desc->N, desc->M, desc->groups, true);
+    *bytes = rts_group_footprint(desc->N, desc->M, desc->groups, true, rts_split_mode(desc->precision));
     return RTS_OK;
 }
 
@@ -103,7 +105,7 @@ int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* i
     if (rc != RTS_OK) return rc;
 
     GProb* p = nullptr;
-    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, d->precision == RTS_PREC_FP16X3, d->flush, d->bn, true, &p,
+    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), d->flush, d->bn, true, &p,
                                st);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
@@ -117,7 +119,7 @@ int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* i
         rts_group_remove_on(batch, tmp, st);
         return rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: copy failed: %s", cudaGetErrorString(e));
     }
-    rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->fp16, p->rs, p->rows_pad, p->a[0], st);
+    rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->mode, p->rs, p->rows_pad, p->a[0], st);
     if (rc == RTS_OK && sync) {
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: %s", cudaGetErrorString(e));
@@ -288,7 +290,7 @@ extern "C" int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc*
     rc = rts_launch_weights_raw(ctx, d_xyz, d_area, (int)M, 0, (int)M, full_area, d->phase, d->g, W, st);
     if (rc != RTS_OK) return rc;
     GProb* p = nullptr;
-    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, d->precision == RTS_PREC_FP16X3, d->flush, d->bn, true, &p);
+    rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), d->flush, d->bn, true, &p);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
     for (int64_t g = 0; g < G; ++g) lam[(size_t)g] = (float)lambda[g];
@@ -298,7 +300,7 @@ extern "C" int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc*
     cudaError_t e = cudaSuccess;
     if (rc == RTS_OK) e = cudaMemcpyAsync(p->lam, lam.data(), (size_t)G * 4, cudaMemcpyHostToDevice, st);
     if (rc == RTS_OK && e == cudaSuccess)
-        rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->fp16, p->rs, p->rows_pad,
+        rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->mode, p->rs, p->rows_pad,
                                   p->a[0], st);
     if (rc == RTS_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
     int64_t new_id = 0;

@@ -451,7 +451,7 @@ int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
                 "rts_scattering_update: null host buffer");
     RTS_REQUIRE(ctx, B_host || lambda == 1.0, RTS_ERR_INVALID_ARGUMENT,
                 "rts_scattering_update: B is required unless lambda == 1");
-    if (precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3) {
+    if (precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3 || precision == RTS_PREC_TF32X3) {
         ctx->solve_ready = false;
         return rts_split_host_call(ctx, precision, illum_host, B_host, lambda, S_host);
     }
@@ -671,7 +671,7 @@ int rts_solve_setup(rts_ctx* ctx, int precision, const double* B_host, double la
                 (long long)ctx->out_start, (long long)ctx->out_end, (long long)ctx->M);
     RTS_REQUIRE(ctx,
                 precision == RTS_PREC_FP64 || precision == RTS_PREC_BF16X3 ||
-                    precision == RTS_PREC_FP16X3,
+                    precision == RTS_PREC_FP16X3 || precision == RTS_PREC_TF32X3,
                 RTS_ERR_INVALID_ARGUMENT, "rts_solve_setup: unknown precision %d", precision);
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_B, B_host, rts_bytes<double>(ctx->N),

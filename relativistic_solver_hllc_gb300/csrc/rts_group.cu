@@ -41,16 +41,16 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn(rts_ctx* ctx)
     return fn;
 }
 
-// 2-D map over interleaved split rows [rows][2*kpad] (16-bit): box of
+// 2-D map over interleaved split rows [rows][units] (16-bit units): box of
 // box_cols halves x box_rows; the MMA operands use 64 x rows with a 128-byte
 // swizzle, the relaxation 8 x 32 unswizzled (16 bytes of each of 32 rows).
-int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t kpad, int box_rows, int box_cols = 64,
+int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t units, int box_rows, int box_cols = 64,
              bool swizzle = true)
 {
     auto enc = encode_fn(ctx);
     if (!enc) return RTS_ERR_CUDA;
-    cuuint64_t dims[2] = {(cuuint64_t)(2 * kpad), (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(2 * kpad * 2)};
+    cuuint64_t dims[2] = {(cuuint64_t)units, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(units * 2)};
     cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1u, 1u};
     CUresult r = enc(reinterpret_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base),
@@ -59,7 +59,7 @@ int make_map(rts_ctx* ctx, void* map, const void* base, int64_t rows, int64_t kp
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return rts_fail(ctx, RTS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for %lld x %lld", (int)r,
-                        (long long)rows, (long long)(2 * kpad));
+                        (long long)rows, (long long)units);
     return RTS_OK;
 }
 
@@ -99,8 +99,8 @@ namespace {
 // frees are stream-ordered: after the work already queued on `st`
 void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
 {
-    const size_t abytes = (size_t)(p->rows_pad * 2 * p->kpad * 2);
-    rts_pfree(ctx, p->wc, (size_t)(p->mpad * 2 * p->kpad * 2), st);
+    const size_t abytes = (size_t)(p->rows_pad * p->units * 2);
+    rts_pfree(ctx, p->wc, (size_t)(p->mpad * p->units * 2), st);
     rts_pfree(ctx, p->cs, (size_t)(2 * p->mpad * 4), st);
     rts_pfree(ctx, p->a[0], abytes, st);
     rts_pfree(ctx, p->a[1], abytes, st);
@@ -147,18 +147,19 @@ int ensure_scratch(rts_batch* b, size_t bytes, cudaStream_t st)
 // source iteration); the table takes a value between the two.  Without it
 // the loss compounds through a relaxed iteration (1.3e-6 after 20 steps on
 // 663,552 x 1000); with it the error stays near the single-evaluation level.
-float rts_group_bias(const rts_ctx* ctx, bool fp16, int flush)
+float rts_group_bias(const rts_ctx* ctx, int mode, int flush)
 {
     if (ctx->split_bias < 0) return 0.0f;
     if (ctx->split_bias > 0) return (float)(ctx->split_bias * 1e-10);
     // mean relative loss of one evaluation, between the first evaluation of
     // rough (lognormal sigma 1..1.5) intensities and the smoother iterates of
     // a relaxed source iteration
-    static const float table[2][2] = {
+    static const float table[3][2] = {
         {6.0e-8f, 8.0e-8f},  // BF16 hi/lo, flush 1 / 2
         {9.0e-8f, 1.8e-7f},  // FP16 hi/lo, flush 1 / 2
+        {9.0e-8f, 1.8e-7f},  // TF32 hi/lo, flush 1 / 2
     };
-    return table[fp16 ? 1 : 0][flush >= 2 ? 1 : 0];
+    return table[mode < 0 || mode > 2 ? 1 : mode][flush >= 2 ? 1 : 0];
 }
 
 // Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
@@ -179,14 +180,15 @@ void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override
     *m_tiles = *rows_pad / G_BM;
 }
 
-int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative)
+int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative, int mode)
 {
     int bn, nt;
     int64_t kpad, mpad, rows_pad, mt;
     const int64_t rows = N * groups;
     rts_group_geometry(M, M, rows, 0, &bn, &nt, &kpad, &mpad, &rows_pad, &mt);
-    int64_t bytes = mpad * 2 * kpad * 2 + 2 * mpad * 4 + 2 * rows_pad * 4 + rows * 4 + groups * 4;
-    bytes += (iterative ? 2 : 1) * rows_pad * 2 * kpad * 2;
+    const int64_t units = (mode == 2 ? 4 : 2) * kpad;
+    int64_t bytes = mpad * units * 2 + 2 * mpad * 4 + 2 * rows_pad * 4 + rows * 4 + groups * 4;
+    bytes += (iterative ? 2 : 1) * rows_pad * units * 2;
     if (iterative) bytes += rows * M * 4;
     return bytes;
 }
@@ -194,9 +196,10 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
 // Creates a problem: allocations, W (phase kernel on the given directions)
 // split into rows, tensor maps.  A rows, B and lambda are filled by the caller.
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev,
-                          int ldw, bool fp16, int flush, int bn_override, bool iterative, GProb** out,
+                          int ldw, int mode, int flush, int bn_override, bool iterative, GProb** out,
                           cudaStream_t st)
 {
+    const bool fp16 = mode == 1;
     rts_ctx* ctx = b->ctx;
     GProb* p = new GProb();
     p->N = N;
@@ -205,8 +208,9 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     p->groups = groups;
     p->rows = N * groups;
     p->fp16 = fp16;
+    p->mode = mode;
     p->flush = std::min(std::max(flush, 1), G_MAX_FLUSH);
-    if (bn_override <= 0 && Mout == Min) bn_override = rts_tuned_bn(ctx, Min, fp16, p->flush);  // 0 if not tuned
+    if (bn_override <= 0 && Mout == Min) bn_override = rts_tuned_bn(ctx, Min, mode, p->flush);  // 0 if not tuned
     rts_group_geometry(Min, Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad, &p->rows_pad,
                        &p->m_tiles);
     int rc;
@@ -219,8 +223,9 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     }                                                                 \
     p->field = (decltype(p->field))q;                                 \
     p->bytes += (nbytes);
-    const size_t abytes = (size_t)(p->rows_pad * 2 * p->kpad * 2);
-    GP_ALLOC(wc, (size_t)(p->mpad * 2 * p->kpad * 2), "split W");
+    p->units = (mode == 2 ? 4 : 2) * p->kpad;
+    const size_t abytes = (size_t)(p->rows_pad * p->units * 2);
+    GP_ALLOC(wc, (size_t)(p->mpad * p->units * 2), "split W");
     GP_ALLOC(cs, (size_t)(2 * p->mpad * 4), "W column scales");
     GP_ALLOC(a[0], abytes, "split Ibar");
     if (iterative) {
@@ -236,12 +241,12 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
     if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
-    rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, fp16, p->wc, p->cs, st);
-    if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->kpad, p->bn);
-    if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->kpad, G_BM);
-    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->kpad, G_BM);
-    if (rc == RTS_OK) rc = make_map(ctx, p->rmaps[0], p->a[0], p->rows_pad, p->kpad, 32, 8, false);
-    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->rmaps[1], p->a[1], p->rows_pad, p->kpad, 32, 8, false);
+    rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs, st);
+    if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->units, p->bn);
+    if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->units, G_BM);
+    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->units, G_BM);
+    if (rc == RTS_OK) rc = make_map(ctx, p->rmaps[0], p->a[0], p->rows_pad, p->units, 32, 8, false);
+    if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->rmaps[1], p->a[1], p->rows_pad, p->units, 32, 8, false);
     if (rc != RTS_OK) {
         free_prob(ctx, p, st);
         return rc;
@@ -322,13 +327,14 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.n_tiles = p->n_tiles;
     g.Mout = (int)p->Mout;
     g.kpad = (int)p->kpad;
-    g.kblocks = (int)(p->kpad / 32);
+    g.kblocks = (int)(p->kpad / (p->mode == 2 ? 16 : 32));
     g.bn = p->bn;
     g.flush = p->flush;
     g.groups = (int)p->groups;
-    g.idesc = rts_ptx::idesc_f16(p->fp16, G_BM, p->bn);
-    g.bias = rts_group_bias(ctx, p->fp16, p->flush);
+    g.idesc = rts_ptx::idesc_split(p->mode, G_BM, p->bn);
+    g.bias = rts_group_bias(ctx, p->mode, p->flush);
     g.fp16 = p->fp16 ? 1 : 0;
+    g.tf32 = p->mode == 2 ? 1 : 0;
     g.cur = p->cur;
     g.relax = relaxes(p, relax) ? 1 : 0;
     g.flip = g.relax;

@@ -18,7 +18,9 @@ struct GProb {
     int64_t N = 0, M = 0, Mout = 0, groups = 1, rows = 0, rows_pad = 0, kpad = 0, mpad = 0;  // M: in-directions
     int bn = 0, n_tiles = 0, flush = 1;
     int64_t m_tiles = 0;
-    bool fp16 = true;
+    bool fp16 = true;        // FP16 split with row / column scales (mode 1)
+    int mode = 1;            // split mode: 0 BF16, 1 FP16, 2 TF32
+    int64_t units = 0;       // 16-bit units per split row: 2*kpad, or 4*kpad for TF32
     uint16_t* wc = nullptr;  // [mpad][2*kpad] split W^T rows
     float* cs = nullptr;     // [2*mpad]: column scale, inverse
     uint16_t* a[2] = {nullptr, nullptr};  // [rows_pad][2*kpad] split Ibar rows (ping-pong)
@@ -38,12 +40,12 @@ struct GProb {
 
 void rts_group_geometry(int64_t Min, int64_t Mout, int64_t rows, int bn_override, int* bn, int* n_tiles, int64_t* kpad,
                         int64_t* mpad, int64_t* rows_pad, int64_t* m_tiles);
-int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative);
+int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative, int mode = 1);
 int rts_group_batch_new(rts_ctx* ctx, rts_batch** out);
 void rts_group_batch_free(rts_batch* b);
 // buffers allocated and initialised on st (null: the scattering stream)
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev, int ldw,
-                          bool fp16, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr);
+                          int mode, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr);
 int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
 GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
 int rts_group_remove(rts_batch* b, int64_t id);
@@ -71,4 +73,4 @@ rts_ctx* rts_group_ctx(rts_batch* b);
 // Forces the device table to be rebuilt before the next launch (after the
 // caller changed cur / S64 / use_B of a problem) and drops a captured graph.
 void rts_group_invalidate(rts_batch* b);
-float rts_group_bias(const rts_ctx* ctx, bool fp16, int flush);
+float rts_group_bias(const rts_ctx* ctx, int mode, int flush);

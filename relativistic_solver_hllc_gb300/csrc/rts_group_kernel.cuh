@@ -38,6 +38,8 @@
 // sets the device flag, every role stops at its next wait, and the kernel
 // drains and exits.
 
+#include <type_traits>
+
 constexpr int G_BM = 128;
 constexpr int G_BN = 256;
 constexpr int G_STAGES = 4;
@@ -70,6 +72,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     uint32_t idesc;
     float bias;           // relative correction of the truncation bias of the sums
     int fp16;
+    int tf32;             // split TF32 operands (kind::tf32, 16 in-directions per K-slice)
     int cur;              // buffer holding the current Ibar
     int relax, residual;
     int flip;             // the step ends in this launch: flip the ping-pong Ibar buffer after it
@@ -120,6 +123,21 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
     *hp = make_uint4(nh[0], nh[1], nh[2], nh[3]);
     *lp = make_uint4(nl[0], nl[1], nl[2], nl[3]);
     return amax > 60000.0f;
+}
+
+// The same for 4 columns of a split TF32 row (hi and lo as FP32, no scale).
+__device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk)
+{
+    const float4 h = *hp, l = *lp;
+    const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+    float nh[4], nl[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float x = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * (hv[j] + lv[j])) : 0.0f;
+        rts_ptx::split_tf32(x, nh[j], nl[j]);
+    }
+    *hp = make_float4(nh[0], nh[1], nh[2], nh[3]);
+    *lp = make_float4(nl[0], nl[1], nl[2], nl[3]);
 }
 
 __global__ void __launch_bounds__(G_THREADS, 1)
@@ -205,44 +223,58 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 const uint32_t idesc = P.idesc;
                 const int nkb = P.kblocks, flush = P.flush;
                 const int nchunks = (nkb + flush - 1) / flush;
-                for (int c = 0; c < nchunks; ++c) {
-                    const uint32_t g = gch + (uint32_t)c;
-                    if ((g & 1u) != me) continue;
-                    const int kb0 = c * flush;
-                    const int f = min(flush, nkb - kb0);
-                    if (g >= 2 && !mbar_wait(acc_empty_bar(me), ((g >> 1) - 1) & 1, flag, FLAG_WAIT_MMA)) {
-                        ok = false;
-                        break;
-                    }
-                    uint32_t ad[G_MAX_FLUSH], st[G_MAX_FLUSH];
-                    for (int j = 0; j < f; ++j) {
-                        const uint32_t i2 = gsl + (uint32_t)(kb0 + j);
-                        st[j] = i2 % G_STAGES;
-                        if (!mbar_wait(full_bar((int)st[j]), (i2 / G_STAGES) & 1, flag, FLAG_WAIT_MMA)) {
+                // the chunk loop, compiled once per MMA kind
+                auto chunks = [&](auto tf32c) {
+                    constexpr bool tf32 = decltype(tf32c)::value;
+                    auto mma = [&](uint64_t a, uint64_t b, uint32_t accumulate) {
+                        if (tf32)
+                            umma_tf32(acc, a, b, idesc, accumulate);
+                        else
+                            umma_f16(acc, a, b, idesc, accumulate);
+                    };
+                    for (int c = 0; c < nchunks; ++c) {
+                        const uint32_t g = gch + (uint32_t)c;
+                        if ((g & 1u) != me) continue;
+                        const int kb0 = c * flush;
+                        const int f = min(flush, nkb - kb0);
+                        if (g >= 2 && !mbar_wait(acc_empty_bar(me), ((g >> 1) - 1) & 1, flag, FLAG_WAIT_MMA)) {
                             ok = false;
                             break;
                         }
-                        ad[j] = smem_base + st[j] * G_STAGE_BYTES;
+                        uint32_t ad[G_MAX_FLUSH], st[G_MAX_FLUSH];
+                        for (int j = 0; j < f; ++j) {
+                            const uint32_t i2 = gsl + (uint32_t)(kb0 + j);
+                            st[j] = i2 % G_STAGES;
+                            if (!mbar_wait(full_bar((int)st[j]), (i2 / G_STAGES) & 1, flag, FLAG_WAIT_MMA)) {
+                                ok = false;
+                                break;
+                            }
+                            ad[j] = smem_base + st[j] * G_STAGE_BYTES;
+                        }
+                        if (!ok) break;
+                        tc_fence_after();
+                        const uint64_t hi0 = 0, hi1 = 32 >> 4, lo0 = 64 >> 4, lo1 = 96 >> 4;
+                        // cross products first (the accumulator starts from zero), hi*hi last
+                        for (int j = 0; j < f; ++j) {
+                            const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
+                            mma(A + hi0, Bd + lo0, j != 0 ? 1u : 0u);
+                            mma(A + lo0, Bd + hi0, 1u);
+                            mma(A + hi1, Bd + lo1, 1u);
+                            mma(A + lo1, Bd + hi1, 1u);
+                        }
+                        for (int j = 0; j < f; ++j) {
+                            const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
+                            mma(A + hi0, Bd + hi0, 1u);
+                            mma(A + hi1, Bd + hi1, 1u);
+                        }
+                        for (int j = 0; j < f; ++j) umma_commit(empty_bar((int)st[j]));
+                        umma_commit(acc_full_bar((int)me));
                     }
-                    if (!ok) break;
-                    tc_fence_after();
-                    const uint64_t hi0 = 0, hi1 = 32 >> 4, lo0 = 64 >> 4, lo1 = 96 >> 4;
-                    // cross products first (the accumulator starts from zero), hi*hi last
-                    for (int j = 0; j < f; ++j) {
-                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
-                        umma_f16(acc, A + hi0, Bd + lo0, idesc, j != 0 ? 1u : 0u);
-                        umma_f16(acc, A + lo0, Bd + hi0, idesc, 1u);
-                        umma_f16(acc, A + hi1, Bd + lo1, idesc, 1u);
-                        umma_f16(acc, A + lo1, Bd + hi1, idesc, 1u);
-                    }
-                    for (int j = 0; j < f; ++j) {
-                        const uint64_t A = smem_desc_sw128(ad[j]), Bd = smem_desc_sw128(ad[j] + G_A_BYTES);
-                        umma_f16(acc, A + hi0, Bd + hi0, idesc, 1u);
-                        umma_f16(acc, A + hi1, Bd + hi1, idesc, 1u);
-                    }
-                    for (int j = 0; j < f; ++j) umma_commit(empty_bar((int)st[j]));
-                    umma_commit(acc_full_bar((int)me));
-                }
+                };
+                if (P.tf32)
+                    chunks(std::true_type{});
+                else
+                    chunks(std::false_type{});
                 gch += (uint32_t)nchunks;
                 gsl += (uint32_t)nkb;
             }
@@ -348,7 +380,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             //   Ibar' = 0.5 Ibar + 0.5 rs[row] * S   (relaxation, split again)
             const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
             const int64_t Nc = P.N, ld = P.ldS;
-            const int Mout = P.Mout, kpad = P.kpad;
+            const int Mout = P.Mout;
             const bool in_row = r < P.rows;
             const int64_t grp = in_row ? r / Nc : 0;
             const int64_t cc = in_row ? r - grp * Nc : 0;
@@ -364,120 +396,151 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             const int kbase = n_tile * bn + 64 * cs;
-            // The relaxation's split rows of each block of 8 columns (16 B hi and
-            // 16 B lo of each of the warp's 32 rows) move by TMA: a 2-D box load
-            // into one of two shared-memory buffers per warp, one block ahead,
-            // and after the update a box store back into the other ping-pong
-            // buffer.  A buffer is refilled only once the store that read it
-            // has finished reading (rows 4*kpad bytes apart would otherwise cost
-            // a line per lane on every access).
+            // The relaxation's split rows move by TMA in units of 16 B hi and
+            // 16 B lo of each of the warp's 32 rows (8 columns of a 16-bit
+            // split, 4 of a TF32 split): a 2-D box load into one of two
+            // shared-memory buffers per warp, one unit ahead, and after the
+            // update a box store back into the other ping-pong buffer.  A buffer
+            // is refilled only once the store that read it has finished reading
+            // (rows 4*kpad bytes apart would otherwise cost a line per lane on
+            // every access).
             const bool want_rel = relax && S64 == nullptr;  // relax implies Mout == M <= kpad
-            const int row0 = m_tile * G_BM + q * 32;
-            const void* map_in = &P.mapR[P.cur];
-            const void* map_out = &P.mapR[P.cur ^ 1];
-            auto fetch = [&](int e0) {
-                const int k0 = kbase + e0;
-                if (!want_rel || k0 >= Mout || e0 >= ncols) return;
-                if (lane == 0) {
-                    const uint32_t b = rel_issued & 1u, dst = rbuf_s + b * 1024u;
-                    const int x = (k0 >> 5) * 64 + (k0 & 31);
-                    bulk_wait_read0();  // the store that last read this buffer
-                    mbar_expect_tx(rel_bar(ew, b), 1024);
-                    tma_load_2d(dst, map_in, x, row0, rel_bar(ew, b));
-                    tma_load_2d(dst + 512u, map_in, x + 32, row0, rel_bar(ew, b));
-                }
-                ++rel_issued;
-            };
             float rmax = 0.0f;
             bool overflow = false;
-            // previous S of a block of 8 columns, loaded one block ahead
-            auto load_old = [&](int e0, float (&o)[8]) {
-                const int k0 = kbase + e0;
-                const int nk = min(8, Mout - k0);
-                if (in_row && nk > 0 && residual && S && e0 < ncols) {
-                    const float* sp = S + (int64_t)k0 * ld;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j, sp += ld) o[j] = j < nk ? *sp : 0.0f;
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) o[j] = 0.0f;
-                }
-            };
-            float old_next[8];
-            load_old(0, old_next);
-            fetch(0);
-#pragma unroll 1
-            for (int e0 = 0; e0 < ncols; e0 += 8) {
-                const int k0 = kbase + e0;
-                const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
-                const bool live_k = in_row && nk > 0;
-                const bool rel = want_rel && nk > 0;  // same for all lanes
-                if (e0 + 8 < ncols) fetch(e0 + 8);
-                float old[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) old[j] = old_next[j];
-                load_old(e0 + 8, old_next);
-                float cin[8];
-                if (fp16) {
-                    const float4 c0 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0));
-                    const float4 c1 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0) + 1);
-                    cin[0] = c0.x, cin[1] = c0.y, cin[2] = c0.z, cin[3] = c0.w;
-                    cin[4] = c1.x, cin[5] = c1.y, cin[6] = c1.z, cin[7] = c1.w;
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) cin[j] = 1.0f;
-                }
-                float v[8];
-                tmem_ld8(last_acc + (uint32_t)e0, v);
-                float snew[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
-                if (live_k) {
-                    if (S64) {
-                        double* dp = S64 + (int64_t)k0 * ld;
-#pragma unroll
-                        for (int j = 0; j < 8; ++j, dp += ld)
-                            if (j < nk) *dp = (double)snew[j];
-                    } else {
-                        float* sp = S + (int64_t)k0 * ld;
-#pragma unroll
-                        for (int j = 0; j < 8; ++j, sp += ld)
-                            if (j < nk) {
-                                *sp = snew[j];
-                                rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
-                            }
+            // the steps, compiled once per split format (columns per relaxation unit)
+            auto run_steps = [&](auto tf32c) {
+                constexpr bool tf32 = decltype(tf32c)::value;
+                constexpr int ucols = tf32 ? 4 : 8;
+                const int row0 = m_tile * G_BM + q * 32;
+                const void* map_in = &P.mapR[P.cur];
+                const void* map_out = &P.mapR[P.cur ^ 1];
+                // units of this warp's columns that hold outputs
+                const int u_real = want_rel ? max(0, min(ncols, Mout - kbase) + ucols - 1) / ucols : 0;
+                auto unit_x = [&](int u) {  // box column (16-bit units) of unit u's high parts
+                    const int k0 = kbase + u * ucols;
+                    return tf32 ? (k0 >> 4) * 64 + (k0 & 15) * 2 : (k0 >> 5) * 64 + (k0 & 31);
+                };
+                int u_next = 0;  // next unit to fetch
+                auto pump = [&](int u_cons) {  // keep one unit fetched beyond the one being consumed
+                    while (u_next < u_real && u_next <= u_cons + 1) {
+                        if (lane == 0) {
+                            const uint32_t b = rel_issued & 1u, dst = rbuf_s + b * 1024u;
+                            const int x = unit_x(u_next);
+                            bulk_wait_read0();  // the store that last read this buffer
+                            mbar_expect_tx(rel_bar(ew, b), 1024);
+                            tma_load_2d(dst, map_in, x, row0, rel_bar(ew, b));
+                            tma_load_2d(dst + 512u, map_in, x + 32, row0, rel_bar(ew, b));
+                        }
+                        ++rel_issued;
+                        ++u_next;
                     }
-                }
-                if (rel) {
-                    // this block's rows: wait for the load, relax this lane's
-                    // row in place (rows outside the problem stay unchanged),
-                    // store the box into the other ping-pong buffer
-                    const uint32_t b = rel_used & 1u;
-                    const bool got = mbar_wait(rel_bar(ew, b), (rel_used >> 1) & 1u, flag, FLAG_WAIT_EPILOGUE);
-                    ++rel_used;
-                    if (!__all_sync(0xffffffffu, got)) {
+                };
+                // previous S of a block of 8 columns, loaded one block ahead
+                auto load_old = [&](int e0, float (&o)[8]) {
+                    const int k0 = kbase + e0;
+                    const int nk = min(8, Mout - k0);
+                    if (in_row && nk > 0 && residual && S && e0 < ncols) {
+                        const float* sp = S + (int64_t)k0 * ld;
+    #pragma unroll
+                        for (int j = 0; j < 8; ++j, sp += ld) o[j] = j < nk ? *sp : 0.0f;
+                    } else {
+    #pragma unroll
+                        for (int j = 0; j < 8; ++j) o[j] = 0.0f;
+                    }
+                };
+                float old_next[8];
+                load_old(0, old_next);
+                pump(-1);
+    #pragma unroll 1
+                for (int e0 = 0; e0 < ncols; e0 += 8) {
+                    const int k0 = kbase + e0;
+                    const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
+                    const bool live_k = in_row && nk > 0;
+                    pump(e0 / ucols);
+                    float old[8];
+    #pragma unroll
+                    for (int j = 0; j < 8; ++j) old[j] = old_next[j];
+                    load_old(e0 + 8, old_next);
+                    float cin[8];
+                    if (fp16) {
+                        const float4 c0 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0));
+                        const float4 c1 = __ldg(reinterpret_cast<const float4*>(cs_inv + k0) + 1);
+                        cin[0] = c0.x, cin[1] = c0.y, cin[2] = c0.z, cin[3] = c0.w;
+                        cin[4] = c1.x, cin[5] = c1.y, cin[6] = c1.z, cin[7] = c1.w;
+                    } else {
+    #pragma unroll
+                        for (int j = 0; j < 8; ++j) cin[j] = 1.0f;
+                    }
+                    float v[8];
+                    tmem_ld8(last_acc + (uint32_t)e0, v);
+                    float snew[8];
+    #pragma unroll
+                    for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
+                    if (live_k) {
+                        if (S64) {
+                            double* dp = S64 + (int64_t)k0 * ld;
+    #pragma unroll
+                            for (int j = 0; j < 8; ++j, dp += ld)
+                                if (j < nk) *dp = (double)snew[j];
+                        } else {
+                            float* sp = S + (int64_t)k0 * ld;
+    #pragma unroll
+                            for (int j = 0; j < 8; ++j, sp += ld)
+                                if (j < nk) {
+                                    *sp = snew[j];
+                                    rmax = fmaxf(rmax, fabsf(snew[j] - old[j]));
+                                }
+                        }
+                    }
+                    // this step's units: wait for the load, relax this lane's row in
+                    // place (rows outside the problem stay unchanged), store the box
+                    // into the other ping-pong buffer
+                    bool stop = false;
+                    for (int ui = 0; ui < 8 / ucols; ++ui) {
+                        const int u = e0 / ucols + ui;
+                        if (u >= u_real) break;
+                        const uint32_t b = rel_used & 1u;
+                        const bool got = mbar_wait(rel_bar(ew, b), (rel_used >> 1) & 1u, flag, FLAG_WAIT_EPILOGUE);
+                        ++rel_used;
+                        if (!__all_sync(0xffffffffu, got)) {
+                            stop = true;
+                            break;
+                        }
+                        uint8_t* rb = rbuf + b * 1024u;
+                        const int nku = min(ucols, Mout - (kbase + u * ucols));
+                        if (in_row) {
+                            if (tf32) {
+                                relax4_tf32(reinterpret_cast<float4*>(rb + 16 * lane),
+                                            reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku);
+                            } else {
+                                uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
+                                uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
+                                if (fp16)
+                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku);
+                                else
+                                    relax8<false>(hp, lp, snew, hrsc, nku);
+                            }
+                        }
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            const int x = unit_x(u);
+                            tma_store_2d(map_out, x, row0, rbuf_s + b * 1024u);
+                            tma_store_2d(map_out, x + 32, row0, rbuf_s + b * 1024u + 512u);
+                            bulk_commit();
+                        }
+                        pump(u);
+                    }
+                    if (stop) {
                         ok = false;
                         break;
                     }
-                    uint8_t* rb = rbuf + b * 1024u;
-                    if (live_k) {
-                        uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
-                        uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
-                        if (fp16)
-                            overflow |= relax8<true>(hp, lp, snew, hrsc, nk);
-                        else
-                            relax8<false>(hp, lp, snew, hrsc, nk);
-                    }
-                    fence_proxy_async_smem();
-                    __syncwarp();
-                    if (lane == 0) {
-                        const int x = (k0 >> 5) * 64 + (k0 & 31);
-                        tma_store_2d(map_out, x, row0, rbuf_s + b * 1024u);
-                        tma_store_2d(map_out, x + 32, row0, rbuf_s + b * 1024u + 512u);
-                        bulk_commit();
-                    }
                 }
-            }
+            };
+            if (P.tf32)
+                run_steps(std::true_type{});
+            else
+                run_steps(std::false_type{});
             release_last();
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {

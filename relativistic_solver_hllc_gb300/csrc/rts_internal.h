@@ -157,19 +157,21 @@ int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_ar
                            double full_area, int phase, double g, double* W, cudaStream_t st);
 
 // Operand preparation of the split-precision path (rts_prepass.cu).
-int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, bool fp16,
+// Split formats of the tensor-core operands: mode 0 BF16, 1 FP16 (scaled), 2 TF32.
+inline int rts_split_mode(int precision) { return precision == RTS_PREC_FP16X3 ? 1 : precision == RTS_PREC_TF32X3 ? 2 : 0; }
+int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
                    uint16_t* Wc, float* cs, cudaStream_t st);
-int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B, bool fp16,
+int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B, int mode,
                            float* rs, int64_t npad, uint16_t* A, cudaStream_t st);
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
-                         bool fp16, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st);
+                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st);
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
-                     bool fp16, double* out, cudaStream_t st);
+                     int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 
 // Tensor-core path (rts_split.cu).
-int rts_tuned_bn(const rts_ctx* ctx, int64_t M, bool fp16, int flush);
+int rts_tuned_bn(const rts_ctx* ctx, int64_t M, int mode, int flush);
 int rts_split_setup(rts_ctx* ctx, int precision);
 int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
 // One evaluation from the device Illum (faces) into the FP64 device S, with

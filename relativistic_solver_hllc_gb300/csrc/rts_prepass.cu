@@ -1,9 +1,12 @@
 // rts_prepass.cu -- operand preparation of the split-precision path.
 //
 // Every tensor-core contraction reads its operands as "interleaved split"
-// rows of 16-bit values: for each group of 32 in-directions, 32 high parts
-// followed by 32 low parts (128 bytes), x*scale = hi + lo.  These kernels
-// build them:
+// rows: for FP16 / BF16, for each group of 32 in-directions 32 high parts
+// followed by 32 low parts (16-bit, 128 bytes), x*scale = hi + lo; for TF32,
+// for each group of 16 in-directions 16 high then 16 low parts (FP32 bit
+// patterns, 128 bytes), no scale.  Sizes are in 16-bit units: a row holds
+// 2*kpad of them (4*kpad for TF32).  The mode argument is 0 BF16, 1 FP16,
+// 2 TF32.  These kernels build them:
 //   * W^T rows (one per out-direction) from the FP64 direction-pair matrix,
 //     with a power-of-two column scale in FP16 mode;
 //   * Ibar rows (one per cell) from the reference's face-layout Illum
@@ -32,18 +35,32 @@ __device__ __forceinline__ float pow2_scale(double m)
 
 // W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
 __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad, int mpad,
-                               int fp16, uint16_t* __restrict__ Wc, float* __restrict__ cs)
+                               int mode, uint16_t* __restrict__ Wc, float* __restrict__ cs)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= mpad) return;
-    uint16_t* row = Wc + (int64_t)k * 2 * kpad;
+    const int units = (mode == 2 ? 4 : 2) * kpad;
+    uint16_t* row = Wc + (int64_t)k * units;
     float* cs_inv = cs + mpad;
     if (k >= Mout) {
-        for (int j = 0; j < 2 * kpad; ++j) row[j] = 0;
+        for (int j = 0; j < units; ++j) row[j] = 0;
         cs[k] = 1.0f;
         cs_inv[k] = 1.0f;
         return;
     }
+    if (mode == 2) {
+        float* rowf = reinterpret_cast<float*>(row);
+        for (int j = 0; j < kpad; ++j) {
+            float hi = 0.0f, lo = 0.0f;
+            if (j < Min) split_tf32((float)W[(int64_t)j * ldw + k], hi, lo);
+            rowf[ilv_hi_tf32(j)] = hi;
+            rowf[ilv_hi_tf32(j) + 16] = lo;
+        }
+        cs[k] = 1.0f;
+        cs_inv[k] = 1.0f;
+        return;
+    }
+    const int fp16 = mode == 1;
     float s = 1.0f;
     if (fp16) {
         double m = 0.0;
@@ -111,7 +128,7 @@ __global__ void rowscale_f32_kernel(const float* __restrict__ ibar, int64_t N, i
 // rows, 256 threads.  `Src` supplies the value of (direction j, row r).
 template <class Src>
 __device__ __forceinline__ void split_tile(const Src& src, int64_t rows, int M, int kpad, const float* __restrict__ rs,
-                                           int fp16, uint16_t* __restrict__ A)
+                                           int mode, uint16_t* __restrict__ A)
 {
     __shared__ float tile[64][33];
     const int j0 = blockIdx.y * 32;
@@ -134,6 +151,24 @@ __device__ __forceinline__ void split_tile(const Src& src, int64_t rows, int M, 
     const int64_t r = r0 + rr;
     if (r >= rows) return;
     const int jbase = (part & 1) * 16;
+    if (mode == 2) {
+        // TF32: the 32 in-directions are two 16-wide groups; part 0/1 the
+        // high parts of group 0/1, part 2/3 their low parts (64 B each)
+        float out[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            float hi, lo;
+            split_tf32(tile[rr][jbase + i], hi, lo);
+            out[i] = (part < 2) ? hi : lo;
+        }
+        float* dst = reinterpret_cast<float*>(A + r * 4 * (int64_t)kpad) + (int64_t)((j0 >> 4) + (part & 1)) * 32 +
+                     (part >= 2 ? 16 : 0);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) d4[i] = make_float4(out[4 * i], out[4 * i + 1], out[4 * i + 2], out[4 * i + 3]);
+        return;
+    }
+    const int fp16 = mode == 1;
     uint16_t out[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -166,22 +201,22 @@ struct F32Src {
 };
 
 __global__ void __launch_bounds__(256) split_faces_kernel(const double* __restrict__ illum, int64_t N, int64_t ld,
-                                                          int M, int kpad, const float* __restrict__ rs, int fp16,
+                                                          int M, int kpad, const float* __restrict__ rs, int mode,
                                                           uint16_t* __restrict__ A)
 {
-    split_tile(FacesSrc{illum, ld}, N, M, kpad, rs, fp16, A);
+    split_tile(FacesSrc{illum, ld}, N, M, kpad, rs, mode, A);
 }
 
 __global__ void __launch_bounds__(256) split_f32_kernel(const float* __restrict__ ibar, int64_t N, int M,
                                                         int64_t rows, int kpad, const float* __restrict__ rs,
-                                                        int fp16, uint16_t* __restrict__ A)
+                                                        int mode, uint16_t* __restrict__ A)
 {
-    split_tile(F32Src{ibar, N, M}, rows, M, kpad, rs, fp16, A);
+    split_tile(F32Src{ibar, N, M}, rows, M, kpad, rs, mode, A);
 }
 
 // Rows back to direction-major FP64 Ibar [groups][M][N].
 __global__ void join_rows_kernel(const uint16_t* __restrict__ A, int64_t N, int M, int64_t rows, int kpad,
-                                 const float* __restrict__ rs_inv, int fp16, double* __restrict__ out)
+                                 const float* __restrict__ rs_inv, int mode, double* __restrict__ out)
 {
     const int64_t total = (int64_t)M * rows;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
@@ -190,8 +225,14 @@ __global__ void join_rows_kernel(const uint16_t* __restrict__ A, int64_t N, int 
         const int64_t rem = i - g * (int64_t)M * N;
         const int64_t j = rem / N, c = rem - j * N;
         const int64_t r = g * N + c;
-        const uint16_t* row = A + r * 2 * (int64_t)kpad;
-        const float x = join_any(fp16 != 0, row[ilv_hi(j)], row[ilv_hi(j) + 32]);
+        float x;
+        if (mode == 2) {
+            const float* rowf = reinterpret_cast<const float*>(A + r * 4 * (int64_t)kpad);
+            x = rowf[ilv_hi_tf32(j)] + rowf[ilv_hi_tf32(j) + 16];
+        } else {
+            const uint16_t* row = A + r * 2 * (int64_t)kpad;
+            x = join_any(mode == 1, row[ilv_hi(j)], row[ilv_hi(j) + 32]);
+        }
         out[i] = (double)x * (double)(rs_inv ? rs_inv[r] : 1.0f);
     }
 }
@@ -217,50 +258,51 @@ int blocks_for(rts_ctx* ctx, int64_t n, int threads)
 
 }  // namespace
 
-int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, bool fp16,
+int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
                    uint16_t* Wc, float* cs, cudaStream_t st)
 {
-    split_w_kernel<<<(mpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, mpad, fp16 ? 1 : 0, Wc, cs);
+    split_w_kernel<<<(mpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, mpad, mode, Wc, cs);
     RTS_CHECK_LAUNCH(ctx, "split_w_kernel");
     ctx->launches++;
     return RTS_OK;
 }
 
 int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B,
-                           bool fp16, float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
+                           int mode, float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
 {
+    const bool fp16 = mode == 1;
     if (fp16) {
         rowscale_faces_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(illum, N, ld, M, B, rs, npad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_faces_kernel");
         ctx->launches++;
     }
     dim3 grid((unsigned)((N + 63) / 64), (unsigned)(kpad / 32));
-    split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, ld, M, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
+    split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, ld, M, kpad, fp16 ? rs : nullptr, mode, A);
     RTS_CHECK_LAUNCH(ctx, "split_faces_kernel");
     ctx->launches++;
     return RTS_OK;
 }
 
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
-                         bool fp16, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st)
+                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st)
 {
+    const bool fp16 = mode == 1;
     if (fp16) {
         rowscale_f32_kernel<<<(unsigned)((rows_pad + 127) / 128), 128, 0, st>>>(ibar, N, M, rows, B, rs, rows_pad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_f32_kernel");
         ctx->launches++;
     }
     dim3 grid((unsigned)((rows + 63) / 64), (unsigned)(kpad / 32));
-    split_f32_kernel<<<grid, 256, 0, st>>>(ibar, N, M, rows, kpad, fp16 ? rs : nullptr, fp16 ? 1 : 0, A);
+    split_f32_kernel<<<grid, 256, 0, st>>>(ibar, N, M, rows, kpad, fp16 ? rs : nullptr, mode, A);
     RTS_CHECK_LAUNCH(ctx, "split_f32_kernel");
     ctx->launches++;
     return RTS_OK;
 }
 
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
-                     bool fp16, double* out, cudaStream_t st)
+                     int mode, double* out, cudaStream_t st)
 {
-    join_rows_kernel<<<blocks_for(ctx, (int64_t)M * rows, 256), 256, 0, st>>>(A, N, M, rows, kpad, rs_inv,
-                                                                              fp16 ? 1 : 0, out);
+    join_rows_kernel<<<blocks_for(ctx, (int64_t)M * rows, 256), 256, 0, st>>>(A, N, M, rows, kpad, rs_inv, mode, out);
     RTS_CHECK_LAUNCH(ctx, "join_rows_kernel");
     ctx->launches++;
     return RTS_OK;

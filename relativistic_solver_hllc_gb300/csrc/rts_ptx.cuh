@@ -130,6 +130,19 @@ __device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64
         : "memory");
 }
 
+// tcgen05.mma kind::tf32 (K = 8 per instruction: 32 bytes of each row, the
+// same bytes as one kind::f16 step).
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 __device__ __forceinline__ void umma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -235,6 +248,14 @@ __host__ __device__ __forceinline__ uint32_t idesc_f16(bool fp16, int m, int n)
     return (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// Instruction descriptor for split mode 0 (BF16, kind::f16), 1 (FP16,
+// kind::f16) or 2 (TF32, kind::tf32: A and B format 2).  D = F32, K-major.
+__host__ __device__ __forceinline__ uint32_t idesc_split(int mode, int m, int n)
+{
+    const uint32_t ab = mode == 1 ? 0u : mode == 0 ? 1u : 2u;
+    return (1u << 4) | (ab << 7) | (ab << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
 // ------------------------------------------------------------- hi / lo split
 __device__ __forceinline__ void split_f16(float x, uint16_t& hi, uint16_t& lo)
 {
@@ -306,5 +327,29 @@ __device__ __forceinline__ float2 join2_any(bool fp16, uint32_t hi2, uint32_t lo
 // offset (in halves) of the high part of in-direction j inside an interleaved
 // split row: per 32 in-directions, 32 high halves then 32 low halves
 __host__ __device__ __forceinline__ int64_t ilv_hi(int64_t j) { return (j >> 5) * 64 + (j & 31); }
+
+// ------------------------------------------------------------ TF32 hi / lo split
+// TF32 keeps FP32's 8-bit exponent and 10 explicit mantissa bits.  x = hi +
+// lo with hi = x rounded to TF32 (round to nearest, ties away) and lo = the
+// rounded remainder, so hi + lo carries 22 significant bits; both are stored
+// as FP32 bit patterns whose low 13 bits are zero (the tensor core reads the
+// upper 19 bits).  Rows of the split operands hold, for each group of 16
+// in-directions, 16 high parts then 16 low parts (128 bytes): the same bytes
+// per K-slice as the 16-bit split, at half the in-directions.
+__device__ __forceinline__ float tf32_round(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo)
+{
+    hi = tf32_round(x);
+    lo = tf32_round(x - hi);
+}
+
+// position of in-direction j's high part in a TF32 split row (FP32 units)
+__host__ __device__ __forceinline__ int64_t ilv_hi_tf32(int64_t j) { return (j >> 4) * 32 + (j & 15); }
 
 }  // namespace rts_ptx

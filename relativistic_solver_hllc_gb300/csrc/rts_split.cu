@@ -19,13 +19,13 @@ namespace {
 int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool iterative, const double* B_dev,
                   double lambda, double* S64, cudaStream_t st)
 {
-    const bool fp16 = precision == RTS_PREC_FP16X3;
+    const int mode = rts_split_mode(precision);
     const int64_t N = ctx->N, Min = ctx->M, Mout = ctx->local();
     const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
     GProb* p = nullptr;
     if (*pb) {
         p = rts_group_find(*pb, *id, nullptr);
-        if (p && (p->fp16 != fp16 || p->N != N || p->M != Min || p->Mout != Mout || (iterative && !p->a[1]) ||
+        if (p && (p->mode != mode || p->N != N || p->M != Min || p->Mout != Mout || (iterative && !p->a[1]) ||
                   p->flush != flush)) {
             int rc = rts_group_remove(*pb, *id);
             if (rc != RTS_OK) return rc;
@@ -36,20 +36,20 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
         if (rc != RTS_OK) return rc;
     }
     if (!p) {
-        int rc = rts_group_new_problem(*pb, N, Min, Mout, 1, ctx->d_W, (int)Mout, fp16, flush, 0, iterative, &p);
+        int rc = rts_group_new_problem(*pb, N, Min, Mout, 1, ctx->d_W, (int)Mout, mode, flush, 0, iterative, &p);
         if (rc != RTS_OK) return rc;
         rc = rts_group_attach(*pb, p, id);
         if (rc != RTS_OK) return rc;
     } else {
         // W may have changed (phase / custom weights): split it again
-        int rc = rts_pp_split_w(ctx, ctx->d_W, (int)Min, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, fp16, p->wc,
+        int rc = rts_pp_split_w(ctx, ctx->d_W, (int)Min, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, mode, p->wc,
                                 p->cs, st);
         if (rc != RTS_OK) return rc;
     }
     p->cur = 0;
     p->S64 = S64;
     p->use_B = B_dev != nullptr;
-    int rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)Min, (int)p->kpad, B_dev, fp16, p->rs, p->rows_pad,
+    int rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)Min, (int)p->kpad, B_dev, mode, p->rs, p->rows_pad,
                                     p->a[0], st);
     if (rc != RTS_OK) return rc;
     if (B_dev) {
@@ -109,24 +109,24 @@ int ensure_pipeline(rts_ctx* ctx)
 
 // The one-problem batch of cell range i with n cells, rebuilt when its shape,
 // precision or flush period changed; W split again when the context's W did.
-int chunk_problem(rts_ctx* ctx, int i, int64_t n, bool fp16, int flush, GProb** out, cudaStream_t st)
+int chunk_problem(rts_ctx* ctx, int i, int64_t n, int mode, int flush, GProb** out, cudaStream_t st)
 {
     rts_split_state& s = ctx->split;
     const int64_t M = ctx->M, Mout = ctx->local();
     int rc;
     GProb* p = s.chunk[i] ? rts_group_find(s.chunk[i], s.chunk_id[i], nullptr) : nullptr;
-    if (p && (p->fp16 != fp16 || p->N != n || p->M != M || p->Mout != Mout || p->flush != flush)) {
+    if (p && (p->mode != mode || p->N != n || p->M != M || p->Mout != Mout || p->flush != flush)) {
         if ((rc = rts_group_remove(s.chunk[i], s.chunk_id[i])) != RTS_OK) return rc;
         p = nullptr;
     }
     if (!s.chunk[i] && (rc = rts_group_batch_new(ctx, &s.chunk[i])) != RTS_OK) return rc;
     if (!p) {
-        rc = rts_group_new_problem(s.chunk[i], n, M, Mout, 1, ctx->d_W, (int)Mout, fp16, flush, 0, false, &p);
+        rc = rts_group_new_problem(s.chunk[i], n, M, Mout, 1, ctx->d_W, (int)Mout, mode, flush, 0, false, &p);
         if (rc != RTS_OK) return rc;
         if ((rc = rts_group_attach(s.chunk[i], p, &s.chunk_id[i])) != RTS_OK) return rc;
         s.chunk_w_version[i] = ctx->w_version;
     } else if (s.chunk_w_version[i] != ctx->w_version) {
-        rc = rts_pp_split_w(ctx, ctx->d_W, (int)M, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, fp16, p->wc, p->cs,
+        rc = rts_pp_split_w(ctx, ctx->d_W, (int)M, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs,
                             st);
         if (rc != RTS_OK) return rc;
         s.chunk_w_version[i] = ctx->w_version;
@@ -152,7 +152,7 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
     int rc = ensure_pipeline(ctx);
     if (rc != RTS_OK) return rc;
     rts_split_state& s = ctx->split;
-    const bool fp16 = precision == RTS_PREC_FP16X3;
+    const int mode = rts_split_mode(precision);
     const bool update = B_host != nullptr && lambda != 1.0;
     const int64_t N = ctx->N, M = ctx->M, Mout = ctx->local();
     const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
@@ -169,7 +169,7 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
         const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
         if (n <= 0) break;
         GProb* p = nullptr;
-        if ((rc = chunk_problem(ctx, i, n, fp16, flush, &p, sc)) != RTS_OK) return rc;
+        if ((rc = chunk_problem(ctx, i, n, mode, flush, &p, sc)) != RTS_OK) return rc;
         const bool changed = p->S64 != ctx->d_S + c0 || p->ldS != N || p->use_B != update || p->cur != 0;
         p->cur = 0;
         p->S64 = ctx->d_S + c0;
@@ -204,7 +204,7 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
             break;
         }
         rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad,
-                                    update ? ctx->d_B + c0 : nullptr, fp16, p->rs, p->rows_pad, p->a[0], sc);
+                                    update ? ctx->d_B + c0 : nullptr, mode, p->rs, p->rows_pad, p->a[0], sc);
         if (rc == RTS_OK && update) rc = rts_pp_f64_to_f32(ctx, ctx->d_B + c0, p->B, n, sc);
         if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, sc);
         if (rc != RTS_OK) break;
@@ -250,7 +250,7 @@ int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host)
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     const int64_t n = p->M * p->N;
     int rc = rts_pp_join_rows(ctx, p->a[p->cur], p->N, (int)p->M, p->rows, (int)p->kpad,
-                              p->fp16 ? p->rs + p->rows_pad : nullptr, p->fp16, ctx->d_S, st);
+                              p->fp16 ? p->rs + p->rows_pad : nullptr, p->mode, ctx->d_S, st);
     if (rc != RTS_OK) return rc;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ibar_host, ctx->d_S, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));

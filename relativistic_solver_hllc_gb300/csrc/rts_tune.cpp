@@ -30,9 +30,9 @@ rts_tune_entry* find_entry(rts_ctx* ctx, int64_t M, int precision, int flush)
 
 }  // namespace
 
-int rts_tuned_bn(const rts_ctx* ctx, int64_t M, bool fp16, int flush)
+int rts_tuned_bn(const rts_ctx* ctx, int64_t M, int mode, int flush)
 {
-    const int prec = fp16 ? RTS_PREC_FP16X3 : RTS_PREC_BF16X3;
+    const int prec = mode == 1 ? RTS_PREC_FP16X3 : mode == 2 ? RTS_PREC_TF32X3 : RTS_PREC_BF16X3;
     const int fl = std::max(flush, 1);
     for (const rts_tune_entry& e : ctx->tune)
         if (e.M == M && e.precision == prec && std::max(e.flush, 1) == fl) return e.bn;
@@ -45,7 +45,8 @@ extern "C" int rts_autotune(rts_ctx* ctx, int64_t M, int precision, int flush, i
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     RTS_REQUIRE(ctx, M >= 1 && M <= 65536, RTS_ERR_INVALID_ARGUMENT, "rts_autotune: M=%lld out of range",
                 (long long)M);
-    RTS_REQUIRE(ctx, precision == RTS_PREC_FP16X3 || precision == RTS_PREC_BF16X3, RTS_ERR_INVALID_ARGUMENT,
+    RTS_REQUIRE(ctx, precision == RTS_PREC_FP16X3 || precision == RTS_PREC_BF16X3 || precision == RTS_PREC_TF32X3,
+                RTS_ERR_INVALID_ARGUMENT,
                 "rts_autotune: precision %d is not a tensor-core precision", precision);
     RTS_REQUIRE(ctx, flush >= 0 && flush <= 2, RTS_ERR_INVALID_ARGUMENT, "rts_autotune: flush %d outside [0,2]", flush);
     if (cells <= 0) cells = (int64_t)ctx->num_sms * 128 * 4;  // four waves of row tiles
@@ -149,7 +150,8 @@ extern "C" int rts_autotune_load(rts_ctx* ctx, const char* path)
         int prec = 0, fl = 0, bn = 0;
         double ms = 0.0;
         if (std::sscanf(line, "%lld %d %d %d %lf", &M, &prec, &fl, &bn, &ms) != 5 || M < 1 ||
-            (prec != RTS_PREC_FP16X3 && prec != RTS_PREC_BF16X3) || fl < 1 || fl > 2 || bn < 16 || bn > 256 ||
+            (prec != RTS_PREC_FP16X3 && prec != RTS_PREC_BF16X3 && prec != RTS_PREC_TF32X3) || fl < 1 || fl > 2 ||
+            bn < 16 || bn > 256 ||
             bn % 16 != 0) {
             rc = rts_fail(ctx, RTS_ERR_INVALID_ARGUMENT, "%s: malformed entry: %s", path, line);
             break;

@@ -85,6 +85,27 @@ def test_batch_relaxation_steps(batch):
     assert rel_err(np.array(res), rres.max(axis=0)) <= 1e-2
 
 
+def test_batch_mixed_precisions_one_launch(batch):
+    """FP16x3, BF16x3 and TF32x3 problems in one grouped launch: the TF32
+    ones use kind::tf32 MMAs over 16-direction K-slices, the others kind::f16
+    over 32-direction slices; every problem is checked against FP64 after
+    relaxed steps."""
+    specs = [(900, 146, 1, PHASE_HG, 0.5, "tf32x3"), (700, 302, 2, PHASE_THOMSON, 0.0, "fp16x3"),
+             (500, 146, 1, PHASE_HG, 0.7, "bf16x3"), (1100, 590, 1, PHASE_THOMSON, 0.0, "tf32x3"),
+             (260, 17, 1, PHASE_HG, 0.3, "tf32x3")]
+    tol = {"fp16x3": 4 * TOL, "tf32x3": 4 * TOL, "bf16x3": 8e-5}
+    ids = []
+    for i, (N, M, G, ph, g, prec) in enumerate(specs):
+        ibar, B, lam = make_inputs(40 + i, N, M, G)
+        ids.append((batch.add(problem_desc(N, M, G, ph, g, precision=prec), ibar, B, lam), ibar, B, lam, M, ph, g, prec))
+    for _ in range(3):
+        batch.step(True)
+    for pid, ibar, B, lam, M, ph, g, prec in ids:
+        S, _ = batch.read(pid)
+        ref, _ = reference(weights(M, ph, g), ibar, B, lam, iters=3, relax=True)
+        assert rel_err(S, ref) <= tol[prec], (prec, M, rel_err(S, ref))
+
+
 def test_graph_replay_equals_eager_steps(ctx):
     N, M = 1100, 146
     ibar, B, lam = make_inputs(3, N, M, 1)

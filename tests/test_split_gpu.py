@@ -4,6 +4,7 @@ oracle, through the C ABI.
 Tolerances (max relative error against FP64, written per precision):
   fp16x3: 1e-6  (scaled FP16 hi/lo split, three products, FP32 accumulate)
   bf16x3: 2e-5  (BF16 hi/lo split: 2^-17 per operand, reported, not the headline)
+  tf32x3: 1e-6  (TF32 hi/lo split, kind::tf32 products, FP32 accumulate; no scaling)
 """
 import numpy as np
 import pytest
@@ -12,9 +13,9 @@ import oracle
 from relativistic_solver_hllc_gb300 import PHASE_HG, TUNE_BIAS
 
 pytestmark = pytest.mark.gpu
-TOL = {"fp16x3": 1e-6, "bf16x3": 2e-5}
-# the split of Ibar alone: FP16 hi+lo keeps 22 bits, BF16 hi+lo 16 bits
-SPLIT_TOL = {"fp16x3": 4e-7, "bf16x3": 1.6e-5}
+TOL = {"fp16x3": 1e-6, "bf16x3": 2e-5, "tf32x3": 1e-6}
+# the split of Ibar alone: FP16 and TF32 hi+lo keep 22 bits, BF16 hi+lo 16 bits
+SPLIT_TOL = {"fp16x3": 4e-7, "bf16x3": 1.6e-5, "tf32x3": 4e-7}
 
 
 def rel_err(a, b):
@@ -28,7 +29,7 @@ def problem(N, M, seed=1, sigma=1.5, indep=False):
     return xyz, area, fa, il, B
 
 
-@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3", "tf32x3"])
 @pytest.mark.parametrize("N,M", [(1000, 64), (333, 17), (700, 200), (260, 300), (128, 1000)])
 def test_single_evaluation(ctx, prec, N, M):
     xyz, area, fa, il, B = problem(N, M, indep=True)
@@ -44,7 +45,7 @@ def test_single_evaluation(ctx, prec, N, M):
     assert abs(r - np.max(np.abs(ref))) <= TOL[prec] * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3", "tf32x3"])
 def test_split_of_ibar(ctx, prec):
     N, M = 500, 96
     xyz, area, fa, il, B = problem(N, M, indep=True)
@@ -55,7 +56,7 @@ def test_split_of_ibar(ctx, prec):
     assert rel_err(ib, oracle.face_mean(il, N, M)) <= SPLIT_TOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3", "tf32x3"])
 def test_source_iteration_with_relaxation(ctx, prec):
     N, M, lam, iters = 900, 120, 0.9, 6
     xyz, area, fa, il, B = problem(N, M)
@@ -67,7 +68,7 @@ def test_source_iteration_with_relaxation(ctx, prec):
     W = oracle.weights_thomson(xyz, area, fa)
     S_ref, r_ref, I_ref = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
     # errors of successive steps compound through a contraction of norm <= 0.95
-    assert rel_err(S, S_ref) <= (1 if prec == "fp16x3" else 4) * TOL[prec]
+    assert rel_err(S, S_ref) <= (4 if prec == "bf16x3" else 1) * TOL[prec]
     assert rel_err(np.array(res[1:]), r_ref[1:]) <= 1e-2
     assert rel_err(ctx.solve_read_ibar(), I_ref) <= 4 * TOL[prec]
     hist = ctx.solve_residual_history(iters)
@@ -104,7 +105,7 @@ def test_truncation_bias_correction(ctx):
         ctx.set_tuning(TUNE_BIAS, -2)
 
 
-@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x3", "tf32x3"])
 def test_host_buffer_entry_point(ctx, prec):
     """rts_scattering_update: H2D Illum + B, tensor-core integral + update, D2H S."""
     N, M, lam = 777, 150, 0.7
