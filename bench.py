@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", default="fp16x3", choices=["fp64", "bf16x3", "fp16x3"])
+    ap.add_argument("--precision", default="fp16x3", choices=["fp64", "bf16x3", "fp16x3", "tf32x3"])
     ap.add_argument("--cells", type=int, default=WORKLOAD["N"])
     ap.add_argument("--dirs", type=int, default=WORKLOAD["M"])
     ap.add_argument("--check", choices=["full", "first", "none"], default="full",
@@ -89,7 +89,9 @@ def run_other_config(args, rank, world, local):
         dtype = "f64"
     elif args.config == 3:
         res = bc.config3(pkg, _native, ctx, torch, K, W, prec)
-        res["bf16x3"] = bc.config3(pkg, _native, ctx, torch, K, W, "bf16x3") if prec != "bf16x3" else None
+        # the configuration names the TF32x3 and split-BF16 paths: both beside the headline precision
+        for other in ("tf32x3", "bf16x3"):
+            res[other] = bc.config3(pkg, _native, ctx, torch, K, W, other) if prec != other else None
         dtype = prec
     elif args.config == 4:
         res = bc.config4(pkg, _native, ctx, torch, K, W, prec)
@@ -419,7 +421,7 @@ def run_ours(args, rank, world, local):
                "sample": f"cells [0,{sample['Ns']}) of the {N}-cell Illum (full strides), all {M} in-directions, "
                          f"out-directions [0,{sample['s']})"}
 
-    dtype = {"fp64": "f64", "bf16x3": "bf16x3", "fp16x3": "fp16x3"}[prec]
+    dtype = {"fp64": "f64", "bf16x3": "bf16x3", "fp16x3": "fp16x3", "tf32x3": "tf32x3"}[prec]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": elapsed / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

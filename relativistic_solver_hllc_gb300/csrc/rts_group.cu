@@ -157,7 +157,7 @@ float rts_group_bias(const rts_ctx* ctx, int mode, int flush)
     static const float table[3][2] = {
         {6.0e-8f, 8.0e-8f},  // BF16 hi/lo, flush 1 / 2
         {9.0e-8f, 1.8e-7f},  // FP16 hi/lo, flush 1 / 2
-        {9.0e-8f, 1.8e-7f},  // TF32 hi/lo, flush 1 / 2
+        {7.5e-8f, 1.1e-7f},  // TF32 hi/lo, flush 1 / 2 (zero mean error over 20 relaxed steps, config 2)
     };
     return table[mode < 0 || mode > 2 ? 1 : mode][flush >= 2 ? 1 : 0];
 }
