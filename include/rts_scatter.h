@@ -405,6 +405,13 @@ int rts_write_direction_file(const char* path, int64_t M, const double* xyz, con
 int rts_read_simple_bin(const char* path, int64_t elem_size, int64_t capacity, void* data, int64_t* count);
 int rts_write_simple_bin(const char* path, int64_t elem_size, int64_t count, const void* data);
 
+/* The radiation part of the solution dump WriteFileSolution
+ * (file_module/writer_bin.cpp:15-44, CUDA build) from the device state, into
+ * directory dir: Illum.bin (face mean of direction 0 per cell), energy.bin,
+ * stream.bin, impuls.bin and, when rts_set_geometry was called, divstream.bin
+ * and divimpuls.bin, each an int32 count then the raw FP64 elements. */
+int rts_write_solution(rts_ctx* ctx, const char* dir);
+
 /* Out-direction partition over np ranks: GetSend / GetDisp
  * (solve_module/solve_utils.cpp:177-202). */
 int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);

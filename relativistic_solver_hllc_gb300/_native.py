@@ -92,6 +92,7 @@ _SIGNATURES = {
     "rts_moments": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "rts_set_geometry": (C.c_int, [_vp, _dp, _dp, _dp]),
     "rts_illum_params": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "rts_write_solution": (C.c_int, [_vp, C.c_char_p]),
     "rts_source_update": (C.c_int, [_vp, _dp, C.c_double, _i64, _i64, C.c_int, _dp]),
     "rts_sync_stream": (C.c_int, [_vp, C.c_int, _i64]),
     "rts_wait": (C.c_int, [_vp, _i64]),
@@ -404,6 +405,11 @@ class Context:
         self._check(self.lib.rts_illum_params(self.h, int(stream), _ptr(e), _ptr(f), _ptr(im), _ptr(ds), _ptr(di)),
                     "rts_illum_params")
         return (e, f.reshape(N, 3), im.reshape(N, 3, 3), ds, None if di is None else di.reshape(N, 3))
+
+    def write_solution(self, directory):
+        """Illum.bin, energy.bin, stream.bin, impuls.bin (and divstream.bin,
+        divimpuls.bin with the geometry) in the reference's file layout."""
+        self._check(self.lib.rts_write_solution(self.h, str(directory).encode()), "rts_write_solution")
 
     def source_update(self, B, lam: float, start: int, end: int, stream: int = STREAM_SCATTERING_1,
                       residual: bool = True):

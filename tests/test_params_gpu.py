@@ -97,3 +97,37 @@ def test_divergence_needs_geometry(ctx):
     assert ds is None and di is None
     with pytest.raises(RtsError):
         ctx.set_geometry(np.zeros((N, 4, 3)), np.ones((N, 4)), np.zeros(N))  # volume must be > 0
+
+
+def read_counted(path, per_cell):
+    """int32 count, then count x per_cell FP64 (WRITE_FILE / WriteSimpleFileBin)."""
+    raw = path.read_bytes()
+    n = int(np.frombuffer(raw[:4], dtype=np.int32)[0])
+    data = np.frombuffer(raw[4:], dtype=np.float64)
+    assert data.size == n * per_cell
+    return n, data.reshape(n, per_cell) if per_cell > 1 else data
+
+
+def test_write_solution_files(ctx, tmp_path):
+    """rts_write_solution writes the radiation part of the reference's
+    WriteFileSolution: direction 0's face mean and the moments, each an int32
+    count then the FP64 elements; the divergences only with the geometry."""
+    N, M = 500, 64
+    il = oracle.illum(9, 0.0, 1.0, N, M, independent_faces=True)
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(il)
+    ctx.write_solution(tmp_path)
+    assert not (tmp_path / "divstream.bin").exists()
+    nrm, fS, vol = oracle.cell_geometry(5, N)
+    ctx.set_geometry(nrm, fS, vol)
+    ctx.write_solution(str(tmp_path) + "/")
+    e, fl, im, ds, di = ctx.illum_params(STREAM_PARAMS)
+    n, I0 = read_counted(tmp_path / "Illum.bin", 1)
+    assert n == N
+    faces = il[: N * 4].reshape(N, 4)
+    assert np.array_equal(I0, (((faces[:, 0] + faces[:, 1]) + faces[:, 2]) + faces[:, 3]) / 4)
+    for name, ref, per in (("energy.bin", e, 1), ("stream.bin", fl, 3), ("impuls.bin", im.reshape(N, 9), 9),
+                           ("divstream.bin", ds, 1), ("divimpuls.bin", di, 3)):
+        n, got = read_counted(tmp_path / name, per)
+        assert n == N and np.array_equal(got, ref.reshape(got.shape)), name
