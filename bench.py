@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--flush", type=int, default=2, choices=[0, 1, 2],
                     help="tensor-core K-slices per FP32 drain (library default 1; 2 halves the drains and "
                          "still meets the 1e-6 gate on this workload, checked in the same run)")
+    ap.add_argument("--moments", action="store_true",
+                    help="time the FP64 moment kernels on the config 2 Illum instead (one JSON line)")
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
                     help="2: the headline source iteration (default); 1, 3, 4, 5: the other configurations")
     return ap.parse_args()
@@ -114,6 +116,41 @@ def run_other_config(args, rank, world, local):
                 "dtype": dtype, "data": "synthetic",
                 "config": {"workload": f"config{args.config}: " + res.pop("workload")}, "result": res,
                 "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_moments(args, rank, world, local):
+    """The FP64 moment kernels (energy/flux, and the fused pass with the
+    impulse tensor and divergences) on the config 2 Illum: one JSON line."""
+    import torch
+
+    import bench_configs as bc
+    import relativistic_solver_hllc_gb300 as pkg
+    from relativistic_solver_hllc_gb300 import _native
+
+    pkg.build_library()
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    clocks = ClockSampler(local)
+    clocks.start()
+    res = bc.moments_pass(pkg, _native, ctx, torch, args.steps, args.warmup, N=args.cells)
+    clk = clocks.stop()
+    peaks, src = load_peaks()
+    hbm = peak_value(peaks, "hbm_gbs") or FALLBACK_PEAKS["hbm_gbs"]
+    m = res["illum_params"]
+    line = {"metric": "FP64 moment pass Gcell·dir/s", "value": args.cells * 1000 / (m["kernel_ms"] / 1e3) / 1e9,
+            "unit": "Gcell·dir/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": m["kernel_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"config 2 Illum ({args.cells} cells x 1000 directions, FP64 faces): moments and "
+                                   "fused divergence pass"},
+            "roofline": {"bound": "fp64", "achieved": m["fp64_tflops"], "peak": FP64_NOMINAL_TFLOPS,
+                         "unit": "TFLOP/s", "frac": m["fp64_tflops"] / FP64_NOMINAL_TFLOPS, "traffic": None,
+                         "hbm_gbs": m["hbm_gbs"], "hbm_frac": m["hbm_gbs"] / hbm,
+                         "peak_source": f"nominal GB300 FP64; HBM {src}"},
+            "result": res, "clocks": clk}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -446,6 +483,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)
+    elif args.moments:
+        run_moments(args, rank, world, local)
     elif args.config != 2:
         run_other_config(args, rank, world, local)
     else:

@@ -127,6 +127,36 @@ def config3(pkg, native, ctx, torch, steps, warmup, precision):
             "autotuned_bn": tuned[0], "autotune_ms": {str(k): v for k, v in tuned[2].items()}}
 
 
+def moments_pass(pkg, native, ctx, torch, steps, warmup, N=663_552):
+    """The FP64 moment kernels on the config 2 Illum (663,552 cells x 1000
+    directions, 21.2 GB resident): energy + flux (rts_moments), and energy,
+    flux, impulse tensor and both divergences in one pass (rts_illum_params,
+    synthetic cell geometry).  Kernel times from CUDA events on the kernels'
+    stream; FP64 flops per (cell, direction): 12 and 59."""
+    M = 1000
+    xyz, area, fa = native.synth_directions(M)
+    ctx.init(xyz, area, fa, N)
+    ctx.synth_illum(1, 0.0, 1.5)
+    rng = np.random.default_rng(3)
+    nrm = rng.normal(size=(N, 4, 3))
+    nrm /= np.linalg.norm(nrm, axis=2, keepdims=True)
+    ctx.set_geometry(nrm, rng.uniform(0.5, 1.0, size=(N, 4)), rng.uniform(0.5, 1.0, size=N))
+    out = {}
+    for name, fn, flops in (("moments", lambda: ctx.moments(), 12),
+                            ("illum_params", lambda: ctx.illum_params(), 59)):
+        for _ in range(warmup):
+            fn()
+        ctx.kernel_timing(True)
+        for _ in range(steps):
+            fn()
+        kms, kn = ctx.kernel_timing(False)
+        sec = kms / max(kn, 1) / 1e3
+        nbytes = N * M * 32 + N * (4 if name == "moments" else 17) * 8
+        out[name] = {"kernel_ms": sec * 1e3, "fp64_tflops": flops * N * M / sec / 1e12,
+                     "hbm_gbs": nbytes / sec / 1e9, "flops_per_cell_dir": flops, "bytes": nbytes}
+    return out
+
+
 def config4_problems(seed=3):
     rng = np.random.default_rng(seed)
     probs = []

@@ -443,9 +443,11 @@ int rts_launch_weights(rts_ctx* ctx)
 int rts_launch_moments(rts_ctx* ctx, cudaStream_t st)
 {
     const int64_t blocks = (ctx->N + MOM_THREADS - 1) / MOM_THREADS;
+    rts_timing_begin(ctx, st);
     moments_kernel<<<(unsigned)blocks, MOM_THREADS, 0, st>>>(ctx->d_illum, ctx->d_xyz, ctx->d_area,
                                                              ctx->N, (int)ctx->M, ctx->full_area,
                                                              ctx->d_energy, ctx->d_flux);
+    rts_timing_end(ctx, st);
     RTS_CHECK_LAUNCH(ctx, "moments_kernel");
     ctx->launches++;
     return RTS_OK;
@@ -456,9 +458,11 @@ int rts_launch_illum_params(rts_ctx* ctx, cudaStream_t st)
     const int64_t blocks = (ctx->N + PAR_THREADS - 1) / PAR_THREADS;
     const double* geo = ctx->d_geo;
     const int64_t N = ctx->N;
+    rts_timing_begin(ctx, st);
     illum_params_kernel<<<(unsigned)blocks, PAR_THREADS, 0, st>>>(
         ctx->d_illum, ctx->d_xyz, ctx->d_area, N, (int)ctx->M, ctx->full_area, geo, geo ? geo + 12 * N : nullptr,
         geo ? geo + 16 * N : nullptr, ctx->d_params);
+    rts_timing_end(ctx, st);
     RTS_CHECK_LAUNCH(ctx, "illum_params_kernel");
     ctx->launches++;
     return RTS_OK;
