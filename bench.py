@@ -156,6 +156,24 @@ def run_moments(args, rank, world, local):
     ctx.close()
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The largest value over all ranks (the slowest rank's time); x itself on
+    one process."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(cells: int, dirs: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job Gcell·dir/s of `world` replicas of the workload, each running
+    `steps` steps, over the slowest rank's time."""
+    return cells * dirs * steps * world / seconds / 1e9
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -367,12 +385,9 @@ def run_ours(args, rank, world, local):
     launches = ctx.launch_count() - launches0
     clk = clocks.stop()
     elapsed = ev0.elapsed_time(ev1) / 1e3
-    if dist:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, dist)
     residuals = ctx.solve_residual_history(K).tolist()
-    value = N * M * K * world / elapsed / 1e9
+    value = replicas_value(N, M, K, world, elapsed)
 
     # accuracy against the FP64 path on identical inputs
     accuracy = None
@@ -418,10 +433,7 @@ def run_ours(args, rank, world, local):
     for _ in range(Ke):
         ctx.scattering_update(prec, illum_host, B, lam, S_host)
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist)
     e2e = {"value": N * M * Ke * world / e2e_s / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": M * N * 4 * 8 + N * 8, "d2h_bytes_per_step": M * N * 8,
            "steps": Ke, "call": "rts_scattering_update (pinned host buffers)"}
