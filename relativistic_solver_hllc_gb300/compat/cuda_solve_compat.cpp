@@ -23,6 +23,13 @@
 // CalculateDivImpuls compute their moments (their kernels are commented out
 // in the reference, cuda/cuda_solve.cu:182,236,259).
 //
+// Precision: every call is FP64, bit-compatible with the reference, unless
+// the RTS_SCATTER_PRECISION environment variable names a tensor-core
+// precision (fp16x3, bf16x3 or tf32x3).  Then the synchronous
+// CalculateIntScattering (host Illum in, host scattering out) runs the split
+// tcgen05 path through rts_scattering_update, to <= 1e-6 relative for fp16x3
+// and tf32x3.  The asynchronous calls on the device-resident Illum stay FP64.
+//
 // Cell geometry: like the reference's InitDevice (cuda/cuda_struct.cu:134-176),
 // the first rank reads normals.bin, squares.bin and volume.bin from the
 // solver's base directory -- glb_files.base_adress when this file is built
@@ -46,6 +53,20 @@ namespace {
 rts_ctx* g_ctx = nullptr;
 int g_device = 0;
 bool g_owns_moments = false;
+
+// RTS_SCATTER_PRECISION: fp64 (default), fp16x3, bf16x3 or tf32x3
+int sync_precision()
+{
+    const char* v = std::getenv("RTS_SCATTER_PRECISION");
+    if (!v) return RTS_PREC_FP64;
+    const std::string s(v);
+    if (s == "fp16x3") return RTS_PREC_FP16X3;
+    if (s == "bf16x3") return RTS_PREC_BF16X3;
+    if (s == "tf32x3") return RTS_PREC_TF32X3;
+    if (s != "fp64" && !s.empty())
+        std::fprintf(stderr, "RTS_SCATTER_PRECISION=%s is not fp64, fp16x3, bf16x3 or tf32x3: using fp64\n", v);
+    return RTS_PREC_FP64;
+}
 
 int report(int rc, const char* where)
 {
@@ -220,6 +241,10 @@ int CalculateIntScatteringAsync(const grid_directions_t& grid_dir, grid_t& grid)
 
 int CalculateIntScattering(const grid_directions_t&, grid_t& grid)
 {
+    const int prec = sync_precision();
+    if (prec != RTS_PREC_FP64)  // lambda = 1: the bare integral at that precision
+        return report(rts_scattering_update(g_ctx, prec, grid.Illum, nullptr, 1.0, grid.scattering),
+                      "CalculateIntScattering");
     return report(rts_scattering(g_ctx, grid.Illum, grid.scattering), "CalculateIntScattering");
 }
 

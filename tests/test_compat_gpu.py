@@ -68,3 +68,33 @@ def test_reference_calling_sequence(native_lib, tmp_path):
     assert np.array_equal(ds_g, _native.read_simple_bin(tmp_path / "divstream2.bin"))
     di_g = _native.read_simple_bin(tmp_path / "divimpuls.bin", dt)["v"]
     assert float(np.max(np.abs(di_g - di) / (term * np.max(np.abs(im), axis=1))[:, None])) <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
+def test_sync_call_at_tensor_precision(native_lib, tmp_path, prec):
+    """RTS_SCATTER_PRECISION switches the shim's synchronous
+    CalculateIntScattering to the split tcgen05 path (1e-6 relative); the
+    asynchronous calls on the device Illum stay FP64 (1e-12)."""
+    exe = build_driver(tmp_path)
+    N, M = 1300, 40
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(21, 0.0, 1.0, N, M, independent_faces=True)
+    _native.write_direction_file(tmp_path / "dirs.txt", xyz, area, fa)
+    _native.write_simple_bin(tmp_path / "Illum.bin", il)
+    nrm, fS, vol = oracle.cell_geometry(22, N)
+    geo = tmp_path / "geo"
+    geo.mkdir()
+    _native.write_simple_bin(geo / "normals.bin", nrm.reshape(N, 12).view(np.dtype([("c", np.float64, 12)])).ravel())
+    _native.write_simple_bin(geo / "squares.bin", fS.ravel())
+    _native.write_simple_bin(geo / "volume.bin", vol)
+    env = {**__import__("os").environ, "RTS_GEOMETRY_DIR": str(geo) + "/", "RTS_SCATTER_PRECISION": prec}
+    res = subprocess.run([str(exe), str(tmp_path / "dirs.txt"), str(tmp_path / "Illum.bin"), str(N), str(tmp_path)],
+                         capture_output=True, text=True, timeout=120, env=env)
+    assert res.returncode == 0, res.stderr
+    ref = oracle.calculate_int_cpu(N, xyz, area, fa, il)
+    S_sync = _native.read_simple_bin(tmp_path / "scattering_sync.bin").reshape(M, N)
+    assert float(np.max(np.abs(S_sync - ref) / ref)) <= 1e-6
+    assert float(np.max(np.abs(S_sync - ref) / ref)) > 1e-12  # it did take the split path
+    S_async = _native.read_simple_bin(tmp_path / "scattering.bin").reshape(M, N)
+    assert float(np.max(np.abs(S_async - ref) / ref)) <= 1e-12
