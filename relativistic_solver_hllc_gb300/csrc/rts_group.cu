@@ -335,6 +335,8 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.bias = rts_group_bias(ctx, p->mode, p->flush);
     g.fp16 = p->fp16 ? 1 : 0;
     g.tf32 = p->mode == 2 ? 1 : 0;
+    // a quarter of the tile per epilogue column slice, so that narrow tiles keep every epilogue warp busy
+    g.sw = std::min(64, (int)round_up((p->bn + 3) / 4, 16));
     g.cur = p->cur;
     g.relax = relaxes(p, relax) ? 1 : 0;
     g.flip = g.relax;

@@ -20,8 +20,10 @@
 //   warps 1, 2   MMA issuers (one thread each); warp 1 also owns TMEM
 //                (512 columns: one 256-column accumulator per issuer);
 //   warps 3..18  drain + epilogue: warp w reads TMEM lanes 32*(w%4).. and a
-//                64-column slice of the tile.  After every chunk of `flush`
-//                K-slices they add the chunk's accumulator into FP32
+//                column slice of the tile (a quarter of it, rounded up to
+//                16 columns, so narrow tiles keep every warp busy).  After
+//                every chunk of `flush` K-slices they add the chunk's
+//                accumulator into FP32
 //                registers (round-to-nearest adds: the tensor core truncates
 //                each accumulate) and release it; the tile's sums go back
 //                into its last accumulator, from which the fused epilogue
@@ -73,6 +75,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     float bias;           // relative correction of the truncation bias of the sums
     int fp16;
     int tf32;             // split TF32 operands (kind::tf32, 16 in-directions per K-slice)
+    int sw;               // columns per epilogue column slice: a quarter of bn rounded up to 16 (at most 64)
     int cur;              // buffer holding the current Ibar
     int relax, residual;
     int flip;             // the step ends in this launch: flip the ping-pong Ibar buffer after it
@@ -282,7 +285,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     } else {
         // ------------------------------------------------------------ drain + epilogue warps
         const int q = warp & 3;                    // TMEM lane quarter
-        const int cs = (warp - G_EPI_WARP0) >> 2;  // 64-column slice of the tile
+        const int cs = (warp - G_EPI_WARP0) >> 2;  // column slice of the tile
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const int ew = warp - G_EPI_WARP0;
         uint8_t* rbuf = smem + G_REL_OFF + (size_t)ew * G_REL_BUF;
@@ -294,7 +297,8 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const GroupProblem& P = probs[find_problem(probs, nprob, t)];
             const int nkb = P.kblocks, flush = P.flush, bn = P.bn;
             const int nchunks = (nkb + flush - 1) / flush;
-            const int ncols = min(64, bn - 64 * cs);  // columns of this warp (multiple of 16; <= 0: none)
+            const int sw = P.sw;                         // columns per slice (multiple of 16, <= 64)
+            const int ncols = min(sw, bn - sw * cs);  // columns of this warp (multiple of 16; <= 0: none)
             const int64_t lt = t - P.tile_begin + P.tile_off;
             const int m_tile = (int)(lt / P.n_tiles), n_tile = (int)(lt % P.n_tiles);
             float run[64];
@@ -305,7 +309,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             for (int c = 0; c < nchunks; ++c) {
                 const uint32_t g = gch + (uint32_t)c;
                 const int a = (int)(g & 1u);
-                const uint32_t acc = tmem + 256u * (uint32_t)a + lane_off + 64u * (uint32_t)cs;
+                const uint32_t acc = tmem + 256u * (uint32_t)a + lane_off + (uint32_t)(sw * cs);
                 bool got = true;
                 if (lane == 0) got = mbar_wait(acc_full_bar(a), (g >> 1) & 1, flag, FLAG_WAIT_EPILOGUE);
                 if (!__shfl_sync(0xffffffffu, got ? 1 : 0, 0)) {
@@ -332,7 +336,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         const int64_t r = (int64_t)m_tile * G_BM + q * 32 + lane;
                         if (r < P.rows) {
                             const int64_t Nc = P.N, ld = P.ldS;
-                            const int Mout = P.Mout, kb0 = n_tile * bn + 64 * cs;
+                            const int Mout = P.Mout, kb0 = n_tile * bn + sw * cs;
                             const int64_t grp = r / Nc;
                             if (P.S32 && P.residual) {
                                 const float* Sp = P.S32 + grp * (int64_t)Mout * ld + (r - grp * Nc);
@@ -395,7 +399,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float bias = P.bias;
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
-            const int kbase = n_tile * bn + 64 * cs;
+            const int kbase = n_tile * bn + sw * cs;
             // The relaxation's split rows move by TMA in units of 16 B hi and
             // 16 B lo of each of the warp's 32 rows (8 columns of a 16-bit
             // split, 4 of a TF32 split): a 2-D box load into one of two
