@@ -460,7 +460,6 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     const int k0 = kbase + e0;
                     const int nk = min(8, Mout - k0);  // valid columns of this block (same for all lanes)
                     const bool live_k = in_row && nk > 0;
-                    pump(e0 / ucols);
                     float old[8];
     #pragma unroll
                     for (int j = 0; j < 8; ++j) old[j] = old_next[j];
@@ -496,6 +495,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                                 }
                         }
                     }
+                    // fetch one unit ahead only now: the buffer it fills was read by
+                    // the previous step's store, which has had the TMEM read and the
+                    // S stores above to finish, so lane 0 rarely waits on it
+                    pump(e0 / ucols);
                     // this step's units: wait for the load, relax this lane's row in
                     // place (rows outside the problem stay unchanged), store the box
                     // into the other ping-pong buffer
