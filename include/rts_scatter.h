@@ -417,6 +417,121 @@ int rts_write_solution(rts_ctx* ctx, const char* dir);
 int rts_partition(int np, int64_t n, int64_t* send, int64_t* disp);
 
 /* ---------------------------------------------------------------------- */
+/* transport sweep: the producer of Illum                                  */
+/* ---------------------------------------------------------------------- */
+
+/* Codes of a face without a neighbour in the pairs array (eBoundaryTypes,
+ * global_def.h:45-51). */
+#define RTS_BOUND_FREE (-1)
+#define RTS_BOUND_LOCK (-2)
+#define RTS_BOUND_OUTSOURCE (-3)
+#define RTS_BOUND_INNER (-4)
+
+/* The medium of GetCurIllum (solve_module/illum/Illum_async.cpp:259-470).
+ * RTS_MEDIUM_SCATTERING, classes 0, 1, 3, 10 and 11:
+ *     k = alpha + beta, ss = s * s_scale, S' = S * i_scale, I0' = I0 * i_scale,
+ *     I = exp(-k ss) (I0' k + (exp(k ss) - 1)(Q + S' beta)) / k     (k > 1e-10)
+ *     I = (1 - ss k)(I0' + ss (Q + S' beta))                       (otherwise)
+ *     result max(I, 0) / i_scale;
+ * RTS_MEDIUM_ABSORPTION, class 2:
+ *     I = I0 exp(-alpha ss) + Q (1 - exp(-alpha ss)) / alpha        (alpha > 1e-15)
+ *     I = I0 (1 - alpha ss) + Q ss                                  (otherwise)
+ *     result max(I, 0).
+ * alpha, beta, Q are per cell; s_scale is 1 (DIST for class 11, 388189e5 for
+ * class 2) and i_scale 1 (RADIATION for class 11).  With radius > 0 the
+ * ball_* coefficients hold at the nodes inside the ball (class 0's source
+ * region). */
+#define RTS_MEDIUM_SCATTERING 0
+#define RTS_MEDIUM_ABSORPTION 1
+typedef struct rts_medium {
+    int mode;
+    int reserved;
+    double s_scale;
+    double i_scale;
+    double ball[3];
+    double radius;
+    double ball_alpha, ball_beta, ball_q;
+} rts_medium;
+
+/* Synthetic mesh (host only, no device work): the unit cube cut into n^3
+ * hexahedra (x fastest), each cut into 6 tetrahedra around its diagonal from
+ * (0,0,0) to (1,1,1); N = 6 n^3 cells.  vert [N][4][3]; pairs [N][4] the
+ * neighbour's cell*4 + face or a boundary code; normals [N][4][3] outward
+ * unit normals, face f opposite vertex {2,0,1,3}[f] (VTK's tetra faces
+ * {0,1,3}, {1,2,3}, {2,0,3}, {0,2,1}).  bound_rule 0: every boundary face
+ * RTS_BOUND_FREE (the reference's Cube variant of SetTypeOfBound,
+ * utils/grid_geometry/geometry_data.cpp:512-517); 1: faces of the x = 0 side
+ * RTS_BOUND_OUTSOURCE, of the x = 1 side RTS_BOUND_FREE, others
+ * RTS_BOUND_LOCK (its Cone variant, :484-504).  tilt != 0 turns the cube about
+ * its centre by a fixed rotation (Rx 0.3, Ry 0.2, Rz 0.1 rad; boundary codes
+ * from the unturned faces) so that no face is parallel to a
+ * spherical-Fibonacci direction.  n in [1, 127]. */
+int rts_mesh_cube(int n, int bound_rule, int tilt, double* vert, int32_t* pairs, double* normals);
+
+/* The mesh of the sweep for the context's N cells (rts_init): vertices
+ * [N][4][3] (vertex.bin), pairs [N][4] (pairs.bin) and outward unit face
+ * normals [N][4][3] (normals.bin), the inputs that make_illum_struct and
+ * build_graph read (make_illum_struct/struct_short_characteristics_main.cpp:
+ * 28-74).  Copied to the device; the per-direction structures are dropped. */
+int rts_sweep_set_mesh(rts_ctx* ctx, const double* vert, const int32_t* pairs, const double* normals);
+
+/* Builds the per-direction structures of the local directions on the
+ * device, the work of make_illum_struct and build_graph: the in/out state of
+ * every face (GetInAndOutFaces, utils/grid_geometry/geometry_solve.cpp:212-227),
+ * the cells in dependency order (build_graph_calculation.cpp:347-513: steps
+ * of cells whose in-faces are all known, each step in ascending cell id),
+ * and for every out-face node (MakeArrayX) the in-face hit going back along
+ * the direction and the distance to it (CalculateNodeValue,
+ * struct_short_characteristics_logic_function.cpp:209-243).  *records (may
+ * be NULL) receives the node count over all local directions, *levels the
+ * largest number of steps of one direction.  RTS_ERR_UNSUPPORTED when a
+ * direction's dependencies form a cycle or a node finds no in-face (a
+ * direction parallel to a face). */
+int rts_sweep_build(rts_ctx* ctx, int64_t* records, int64_t* levels);
+
+/* The same structures from the reference's make_illum_struct / build_graph
+ * files of local direction d: order [N] (graph<d>.bin), states [N]
+ * (state_face<d>.bin, bit f set for an in-face) and the LocX0<d>.bin records
+ * (cell_local, global_def.h:101-108: FP64 s at byte 0, uint8 in-face id at
+ * byte 24, 32-byte stride), `count` of them in the file's order.  Every
+ * local direction must be imported (or rts_sweep_build called) before
+ * rts_sweep. */
+int rts_sweep_import_direction(rts_ctx* ctx, int64_t d, const int32_t* order, const int32_t* states,
+                               const void* locx0, int64_t count);
+
+/* The structures of local direction d in the reference's file layouts: order
+ * [N] (graph<d>.bin: cells in dependency order), states [N] (state_face<d>.bin)
+ * and, when capacity >= *count, the LocX0<d>.bin records (32 bytes each: FP64 s,
+ * the 2-D x0 left zero -- the sweep does not read it -- and the uint8 in-face
+ * id at byte 24) in the order of `order`.  Any output may be NULL; *count
+ * receives the record count. */
+int rts_sweep_export_direction(rts_ctx* ctx, int64_t d, int32_t* order, int32_t* states, void* locx0,
+                               int64_t capacity, int64_t* count);
+
+/* Medium coefficients per cell (alpha, beta, Q: [N] FP64 host arrays) and the
+ * intensities of boundary codes -1..-4 (bc [4]; NULL: 0, 0, 1, 0 as
+ * BoundaryConditions, solve_module/illum/illum_utils.cpp:407-474). */
+int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const double* alpha, const double* beta,
+                         const double* Q, const double* bc);
+
+/* One sweep of every local direction (the direction loops of
+ * MPI_CalculateIllumAsync, solve_module/illum/Illum_async.cpp:726-783 and
+ * 831-885) on `stream`: reads the device scattering array [local][N] and
+ * writes the face means of the local directions' rows of the device Illum
+ * (ReCalcIllum, :472-510).  *norm (may be NULL) receives ReCalcIllum's
+ * max |old - new| / new over all faces (-1 if every term was NaN), which
+ * synchronises the stream. */
+int rts_sweep(rts_ctx* ctx, int stream, double* norm);
+
+/* The source iteration of MPI_CalculateIllumAsync (Illum_async.cpp:615-1060)
+ * on the device: repeat { sweep; if max_iter > 1, the scattering integral of
+ * the new Illum into the device scattering array at `precision`
+ * (rts_precision) } while norm > accuracy and fewer than max_iter sweeps ran.
+ * norms [max_iter] (may be NULL) receives each sweep's norm, *iters the
+ * sweeps run.  On RTS_STREAM_SCATTERING_1; one 8-byte read-back per sweep. */
+int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, int64_t* iters, double* norms);
+
+/* ---------------------------------------------------------------------- */
 /* instrumentation                                                         */
 /* ---------------------------------------------------------------------- */
 

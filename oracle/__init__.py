@@ -36,16 +36,17 @@ _u64 = C.c_uint64
 
 
 def build(force: bool = False) -> Path:
-    """Compile the C restatement (gcc -O3 -fopenmp) into oracle/_build/liborc.so."""
-    src = ORACLE_DIR / "scatter_oracle.c"
+    """Compile the C restatements (gcc -O3 -fopenmp) into oracle/_build/liborc.so."""
+    srcs = [ORACLE_DIR / "scatter_oracle.c", ORACLE_DIR / "sweep_oracle.c"]
     BUILD_DIR.mkdir(exist_ok=True)
-    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= src.stat().st_mtime:
+    if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return LIB_PATH
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         raise RuntimeError("no C compiler found for the oracle")
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    cmd = [cc, "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", str(src), "-o", str(tmp), "-lm"]
+    cmd = [cc, "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", *map(str, srcs), "-o", str(tmp),
+           "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
@@ -89,6 +90,18 @@ _SIG = {
     "orc_get_send": (None, [C.c_int, C.c_int, _ip]),
     "orc_get_disp": (None, [C.c_int, C.c_int, _ip]),
     "orc_max_threads": (C.c_int, []),
+    # transport sweep (sweep_oracle.c)
+    "orc_cube_cells": (_i64, [C.c_int]),
+    "orc_cube_mesh": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, C.c_void_p, _dp]),
+    "orc_face_normals": (None, [_i64, _dp, _dp]),
+    "orc_sweep_nodes": (None, [_i64, _dp, _dp]),
+    "orc_face_states": (None, [_i64, _dp, _dp, C.c_void_p]),
+    "orc_sweep_graph": (_i64, [_i64, C.c_void_p, C.c_void_p, C.c_void_p, _i64p]),
+    "orc_sweep_x0": (_i64, [_i64, _dp, _dp, _dp, C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),
+    "orc_sweep_dir": (C.c_double, [_i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _dp, C.c_void_p, _dp,
+                                   C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "orc_sweep_all": (C.c_double, [_i64, _i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _i64p, _dp,
+                                   C.c_void_p, _dp, C.c_void_p, _dp, _dp, _dp, _dp, _dp, C.c_int]),
 }
 
 _lib = None
@@ -277,6 +290,133 @@ def get_send_disp(np_: int, n: int):
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+# ---------------------------------------------------------------- transport sweep
+BOUND_FREE, BOUND_LOCK, BOUND_OUTSOURCE, BOUND_INNER = -1, -2, -3, -4
+DEFAULT_BC = (0.0, 0.0, 1.0, 0.0)  # intensity of boundary codes -1..-4 (BoundaryConditions)
+
+
+class Medium(C.Structure):
+    """GetCurIllum's medium: mode 0 scattering form, 1 absorption form."""
+    _fields_ = [("mode", C.c_int), ("reserved", C.c_int), ("s_scale", C.c_double), ("i_scale", C.c_double),
+                ("ball", C.c_double * 3), ("radius", C.c_double), ("ball_alpha", C.c_double),
+                ("ball_beta", C.c_double), ("ball_q", C.c_double)]
+
+
+def medium(mode=0, s_scale=1.0, i_scale=1.0, ball=(0.0, 0.0, 0.0), radius=0.0, ball_coef=(0.0, 0.0, 0.0)) -> Medium:
+    m = Medium()
+    m.mode, m.s_scale, m.i_scale = mode, s_scale, i_scale
+    m.ball[:] = list(ball)
+    m.radius = radius
+    m.ball_alpha, m.ball_beta, m.ball_q = ball_coef
+    return m
+
+
+def cube_mesh(n: int, bound_rule: int = 1, tilt: bool = True):
+    """Unit cube, n^3 hexahedra x 6 tetrahedra: (vert [N][4][3], pairs [N][4], normals [N][4][3])."""
+    N = lib().orc_cube_cells(n)
+    vert = np.empty((N, 4, 3))
+    pairs = np.empty((N, 4), dtype=np.int32)
+    normals = np.empty((N, 4, 3))
+    if lib().orc_cube_mesh(n, bound_rule, int(tilt), _p(vert), pairs.ctypes.data, _p(normals)) != 0:
+        raise ValueError(f"cube mesh n={n} out of range")
+    return vert, pairs, normals
+
+
+def face_normals(vert) -> np.ndarray:
+    vert = np.ascontiguousarray(vert, dtype=np.float64)
+    out = np.empty_like(vert)
+    lib().orc_face_normals(vert.shape[0], _p(vert), _p(out))
+    return out
+
+
+def sweep_nodes(vert) -> np.ndarray:
+    vert = np.ascontiguousarray(vert, dtype=np.float64)
+    nodes = np.empty((vert.shape[0], 4, 3, 3))
+    lib().orc_sweep_nodes(vert.shape[0], _p(vert), _p(nodes))
+    return nodes
+
+
+def face_states(normals, direction) -> np.ndarray:
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    d = np.ascontiguousarray(direction, dtype=np.float64)
+    st = np.empty(normals.shape[0], dtype=np.int32)
+    lib().orc_face_states(normals.shape[0], _p(normals), _p(d), st.ctypes.data)
+    return st
+
+
+def sweep_graph(pairs, states):
+    """build_graph's order for one direction: (order [N], level offsets [L+1])."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    states = np.ascontiguousarray(states, dtype=np.int32)
+    N = states.shape[0]
+    order = np.empty(N, dtype=np.int32)
+    off = np.empty(N + 1, dtype=np.int64)
+    L = lib().orc_sweep_graph(N, pairs.ctypes.data, states.ctypes.data, order.ctypes.data,
+                              off.ctypes.data_as(_i64p))
+    if L < 0:
+        raise RuntimeError("sweep graph has a dependency cycle")
+    return order, off[: L + 1].copy()
+
+
+def sweep_x0(vert, normals, nodes, order, states, direction):
+    """LocX0 records of one direction in sweep order: (s [n], in-face [n])."""
+    vert = np.ascontiguousarray(vert, dtype=np.float64)
+    normals = np.ascontiguousarray(normals, dtype=np.float64)
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    N = vert.shape[0]
+    d = np.ascontiguousarray(direction, dtype=np.float64)
+    s = np.empty(9 * N)
+    face = np.empty(9 * N, dtype=np.int8)
+    n = lib().orc_sweep_x0(N, _p(vert), _p(normals), _p(nodes), np.ascontiguousarray(order, np.int32).ctypes.data,
+                           np.ascontiguousarray(states, np.int32).ctypes.data, _p(d), _p(s), face.ctypes.data)
+    if n < 0:
+        raise RuntimeError(f"no in-face found for record {-n - 1}")
+    return s[:n].copy(), face[:n].copy()
+
+
+class SweepStructures:
+    """Per-direction structures of a mesh (make_illum_struct + build_graph)."""
+
+    def __init__(self, vert, pairs, normals, xyz):
+        self.vert = np.ascontiguousarray(vert, dtype=np.float64)
+        self.pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+        self.normals = np.ascontiguousarray(normals, dtype=np.float64)
+        self.nodes = sweep_nodes(self.vert)
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self.N, self.D = self.vert.shape[0], xyz.shape[0]
+        self.order = np.empty((self.D, self.N), dtype=np.int32)
+        self.states = np.empty((self.D, self.N), dtype=np.int32)
+        self.levels = []
+        s_parts, f_parts, off = [], [], [0]
+        for d in range(self.D):
+            self.states[d] = face_states(self.normals, xyz[d])
+            self.order[d], lv = sweep_graph(self.pairs, self.states[d])
+            self.levels.append(lv)
+            s, f = sweep_x0(self.vert, self.normals, self.nodes, self.order[d], self.states[d], xyz[d])
+            s_parts.append(s)
+            f_parts.append(f)
+            off.append(off[-1] + s.shape[0])
+        self.rec_off = np.array(off, dtype=np.int64)
+        self.s = np.concatenate(s_parts)
+        self.face = np.concatenate(f_parts)
+
+
+def sweep(st: SweepStructures, S, alpha, beta, Q, illum, md: Medium | None = None, bc=DEFAULT_BC,
+          use_nodes: bool | None = None, nthreads: int = 0) -> float:
+    """Sweep every direction of `st` in place on illum [D][N][4] (FP64);
+    S [D][N].  Returns ReCalcIllum's max norm."""
+    md = md if md is not None else medium()
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    a, b, q = (np.ascontiguousarray(x, dtype=np.float64) for x in (alpha, beta, Q))
+    bcv = np.ascontiguousarray(bc, dtype=np.float64)
+    assert illum.dtype == np.float64 and illum.flags.c_contiguous and illum.size == st.D * st.N * 4
+    use_nodes = md.radius > 0 if use_nodes is None else use_nodes
+    nodes = st.nodes.ctypes.data if use_nodes else None
+    return lib().orc_sweep_all(st.N, st.D, st.pairs.ctypes.data, nodes, st.order.ctypes.data, st.states.ctypes.data,
+                               st.rec_off.ctypes.data_as(_i64p), _p(st.s), st.face.ctypes.data, _p(S),
+                               C.byref(md), _p(a), _p(b), _p(q), _p(bcv), _p(illum), nthreads)
 
 
 # ---------------------------------------------------------------- reference

@@ -19,10 +19,20 @@ from ._native import (  # noqa: F401
     STREAM_SCATTERING_2,
     TUNE_BIAS,
     TUNE_FLUSH,
+    BOUND_FREE,
+    BOUND_INNER,
+    BOUND_LOCK,
+    BOUND_OUTSOURCE,
+    LOCX0_DTYPE,
+    MEDIUM_ABSORPTION,
+    MEDIUM_SCATTERING,
     Batch,
     Context,
+    Medium,
     RtsError,
     header_symbols,
     load_library,
+    medium,
+    mesh_cube,
 )
 from .build import build_library  # noqa: F401

@@ -120,7 +120,41 @@ _SIGNATURES = {
     "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "rts_launch_count": (C.c_int, [_vp, C.POINTER(_i64)]),
     "rts_kernel_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(_i64)]),
+    "rts_mesh_cube": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _dp]),
+    "rts_sweep_set_mesh": (C.c_int, [_vp, _dp, _vp, _dp]),
+    "rts_sweep_build": (C.c_int, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
+    "rts_sweep_import_direction": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _i64]),
+    "rts_sweep_export_direction": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _i64, C.POINTER(_i64)]),
+    "rts_sweep_set_medium": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _dp]),
+    "rts_sweep": (C.c_int, [_vp, C.c_int, _dp]),
+    "rts_illum_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.POINTER(_i64), _dp]),
 }
+
+BOUND_FREE, BOUND_LOCK, BOUND_OUTSOURCE, BOUND_INNER = -1, -2, -3, -4
+MEDIUM_SCATTERING = 0
+MEDIUM_ABSORPTION = 1
+
+
+class Medium(C.Structure):
+    """rts_medium: GetCurIllum's medium (see include/rts_scatter.h)."""
+    _fields_ = [("mode", C.c_int), ("reserved", C.c_int), ("s_scale", C.c_double), ("i_scale", C.c_double),
+                ("ball", C.c_double * 3), ("radius", C.c_double), ("ball_alpha", C.c_double),
+                ("ball_beta", C.c_double), ("ball_q", C.c_double)]
+
+
+def medium(mode=MEDIUM_SCATTERING, s_scale=1.0, i_scale=1.0, ball=(0.0, 0.0, 0.0), radius=0.0,
+           ball_coef=(0.0, 0.0, 0.0)) -> Medium:
+    m = Medium()
+    m.mode, m.s_scale, m.i_scale = mode, s_scale, i_scale
+    m.ball[:] = list(ball)
+    m.radius = radius
+    m.ball_alpha, m.ball_beta, m.ball_q = ball_coef
+    return m
+
+
+# byte layout of the reference's cell_local records (LocX0<k>.bin)
+LOCX0_DTYPE = np.dtype({"names": ["s", "x0", "in_face_id"], "formats": [np.float64, (np.float64, 2), np.uint8],
+                        "offsets": [0, 8, 24], "itemsize": 32})
 
 
 def synth_directions(M: int):
@@ -175,6 +209,18 @@ def write_simple_bin(path, data: np.ndarray):
     a = np.ascontiguousarray(data)
     _status(load_library().rts_write_simple_bin(str(path).encode(), a.dtype.itemsize, a.size, a.ctypes.data_as(_vp)),
             "rts_write_simple_bin")
+
+
+def mesh_cube(n: int, bound_rule: int = 1, tilt: bool = True):
+    """Synthetic tetrahedral mesh of the unit cube (host only): vert [N][4][3],
+    pairs [N][4] int32, normals [N][4][3]."""
+    N = 6 * n * n * n
+    vert = np.empty((N, 4, 3))
+    pairs = np.empty((N, 4), dtype=np.int32)
+    normals = np.empty((N, 4, 3))
+    _status(load_library().rts_mesh_cube(int(n), int(bound_rule), int(tilt), _ptr(vert), pairs.ctypes.data,
+                                         _ptr(normals)), "rts_mesh_cube")
+    return vert, pairs, normals
 
 
 def partition(np_: int, n: int):
@@ -553,6 +599,66 @@ class Context:
                                                 float(a), float(b), int(i0), int(n),
                                                 out.ctypes.data_as(C.POINTER(C.c_float))), "rts_synth_host_f32")
         return out
+
+    # -- transport sweep ------------------------------------------------
+    def sweep_set_mesh(self, vert, pairs, normals):
+        v = _f64(vert, (self.N, 4, 3))
+        p = np.ascontiguousarray(pairs, dtype=np.int32)
+        nrm = _f64(normals, (self.N, 4, 3))
+        if p.size != 4 * self.N:
+            raise ValueError("pairs must hold N*4 entries")
+        self._check(self.lib.rts_sweep_set_mesh(self.h, _ptr(v), p.ctypes.data, _ptr(nrm)), "rts_sweep_set_mesh")
+
+    def sweep_build(self):
+        """Per-direction structures on the device: (node records, largest step count)."""
+        rec, lev = _i64(), _i64()
+        self._check(self.lib.rts_sweep_build(self.h, C.byref(rec), C.byref(lev)), "rts_sweep_build")
+        return rec.value, lev.value
+
+    def sweep_import_direction(self, d: int, order, states, locx0):
+        o = np.ascontiguousarray(order, dtype=np.int32)
+        st = np.ascontiguousarray(states, dtype=np.int32)
+        rec = np.asarray(locx0)
+        if rec.dtype.names:  # structured: lay the fields out as cell_local
+            rec = rec.astype(LOCX0_DTYPE)
+        rec = np.ascontiguousarray(rec)
+        if rec.dtype.itemsize != 32:
+            raise ValueError("LocX0 records are 32 bytes")
+        self._check(self.lib.rts_sweep_import_direction(self.h, int(d), o.ctypes.data, st.ctypes.data,
+                                                        rec.ctypes.data if rec.size else None, rec.shape[0]),
+                    "rts_sweep_import_direction")
+
+    def sweep_export_direction(self, d: int):
+        """(order [N], states [N], LocX0 records [n] of LOCX0_DTYPE) of local direction d."""
+        n = _i64()
+        self._check(self.lib.rts_sweep_export_direction(self.h, int(d), None, None, None, 0, C.byref(n)),
+                    "rts_sweep_export_direction")
+        order = np.empty(self.N, dtype=np.int32)
+        states = np.empty(self.N, dtype=np.int32)
+        rec = np.zeros(n.value, dtype=LOCX0_DTYPE)
+        self._check(self.lib.rts_sweep_export_direction(self.h, int(d), order.ctypes.data, states.ctypes.data,
+                                                        rec.ctypes.data, n.value, C.byref(n)),
+                    "rts_sweep_export_direction")
+        return order, states, rec
+
+    def sweep_set_medium(self, md: Medium, alpha, beta, Q, bc=None):
+        a, b, q = (_f64(x, (self.N,)) for x in (alpha, beta, Q))
+        bcv = None if bc is None else _f64(bc, (4,))
+        self._check(self.lib.rts_sweep_set_medium(self.h, C.byref(md), _ptr(a), _ptr(b), _ptr(q), _ptr(bcv)),
+                    "rts_sweep_set_medium")
+
+    def sweep(self, stream: int = STREAM_SCATTERING_1, read_norm: bool = True):
+        out = C.c_double(0.0)
+        self._check(self.lib.rts_sweep(self.h, int(stream), C.byref(out) if read_norm else None), "rts_sweep")
+        return out.value if read_norm else None
+
+    def illum_solve(self, precision="fp64", max_iter: int = 1, accuracy: float = 1e-5):
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        norms = np.zeros(max_iter)
+        it = _i64()
+        self._check(self.lib.rts_illum_solve(self.h, prec, int(max_iter), float(accuracy), C.byref(it), _ptr(norms)),
+                    "rts_illum_solve")
+        return norms[: it.value].copy()
 
     def synth_illum(self, seed: int, mu: float, sigma: float, independent_faces: bool = False):
         self._check(

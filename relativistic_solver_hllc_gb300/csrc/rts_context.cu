@@ -96,6 +96,7 @@ static void free_grid(rts_ctx* ctx)
 {
     const int64_t loc = ctx->local();
     rts_split_free(ctx);
+    rts_sweep_free(ctx);
     rts_dfree(ctx, ctx->d_illum, rts_bytes<double>(ctx->M * ctx->N * 4));
     rts_dfree(ctx, ctx->d_S, rts_bytes<double>(loc * ctx->N));
     rts_dfree(ctx, ctx->d_W, rts_bytes<double>(ctx->M * loc));

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "rts_scatter.h"
@@ -63,6 +64,45 @@ struct rts_split_state {
     cudaEvent_t ev_start = nullptr, ev_in[RTS_HOST_CHUNKS] = {}, ev_done[RTS_HOST_CHUNKS] = {};
 };
 
+// Device state of the transport sweep (rts_sweep.cu): the mesh, the
+// per-direction structures of the local directions and the medium.  The unit
+// of work is an out-face of a cell (its 3 nodes); per local direction d:
+//   items[d]  out-faces in dependency order: cell << 8 | face << 6 | the
+//             in-faces of its 3 nodes (2 bits each)
+//   recs[d]   3 node distances per item (the LocX0 records' s, same order)
+//   steps[d]  item offsets of the dependency steps (nsteps[d] + 1 entries)
+//   bnd[d]    boundary in-faces, cell * 4 + face (nbnd[d] of them)
+struct rts_sweep_state {
+    int64_t N = 0, D = 0;            // cells, local directions
+    std::vector<double> h_vert, h_normals;  // host copies for the builder
+    std::vector<int32_t> h_pairs;
+    double* d_vert = nullptr;        // [N][4][3]
+    int32_t* d_pairs = nullptr;      // [N][4]
+    double* d_normals = nullptr;     // [N][4][3]
+    double* d_nodes = nullptr;       // [N][4][3][3] (MakeArrayX)
+    uint32_t** d_items = nullptr;    // device pointer tables [D]
+    double** d_recs = nullptr;
+    int32_t** d_steps = nullptr;
+    uint32_t** d_bnd = nullptr;
+    int32_t* d_nsteps = nullptr;     // [D]
+    int32_t* d_nbnd = nullptr;       // [D]
+    std::vector<uint32_t*> h_items;  // host copies of the tables
+    std::vector<double*> h_recs;
+    std::vector<int32_t*> h_steps;
+    std::vector<uint32_t*> h_bnd;
+    std::vector<int32_t> h_nsteps, h_nbnd;
+    std::vector<int64_t> h_nitems;
+    std::vector<std::pair<void*, size_t>> blocks;  // allocations behind the tables
+    std::vector<char> have;          // direction d built or imported
+    double* d_med = nullptr;         // [N][4] alpha, beta, Q, 0
+    rts_medium md{};
+    double bc[4] = {0.0, 0.0, 1.0, 0.0};
+    bool has_medium = false;
+    unsigned long long* d_norm = nullptr;  // norm bits + 1 (0: no term)
+    int64_t records = 0, max_levels = 0;
+};
+void rts_sweep_free(rts_ctx* ctx);
+
 struct rts_ctx {
     int device = 0;
     int num_sms = 0;
@@ -119,6 +159,7 @@ struct rts_ctx {
     int64_t serve_budget = 0;    // tiles per step for policy 1 (0: 8 waves of the SMs)
     int serve_slack = 500;       // policy 1 deadline: arrival + serve_slack / 100 x estimated isolated time
     std::vector<rts_tune_entry> tune;  // rts_autotune results, used for problems created with bn = 0
+    rts_sweep_state* sweep = nullptr;  // transport sweep (rts_sweep_set_mesh)
 
     // instrumentation
     int64_t launches = 0;        // kernels launched by this context
@@ -178,6 +219,9 @@ int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
 // the source update when B != nullptr; local out-directions [0, local).
 int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, const double* B_host, double lambda,
                         double* S_host);
+// One evaluation from the device Illum (faces) into the FP64 device S for
+// every local out-direction, no host copies (the sweep's source iteration).
+int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st);
 int rts_split_read(rts_ctx* ctx, double* S_host);
 int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host);
 void rts_split_free(rts_ctx* ctx);

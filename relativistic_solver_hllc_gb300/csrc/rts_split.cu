@@ -225,6 +225,39 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
     return RTS_OK;
 }
 
+// The same cell ranges as the host-buffer call, on the device Illum and into
+// the device S, all on `st` (no copies, no host synchronisation).
+int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
+{
+    RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
+    rts_split_state& s = ctx->split;
+    const int mode = rts_split_mode(precision);
+    const int64_t N = ctx->N, M = ctx->M;
+    const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
+    const int64_t tiles = (N + 127) / 128;
+    const int nch = (int)std::min<int64_t>(RTS_HOST_CHUNKS, tiles);
+    const int64_t csz = (tiles + nch - 1) / nch * 128;
+    int rc;
+    for (int i = 0; i < nch; ++i) {
+        const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
+        if (n <= 0) break;
+        GProb* p = nullptr;
+        if ((rc = chunk_problem(ctx, i, n, mode, flush, &p, st)) != RTS_OK) return rc;
+        const bool changed = p->S64 != ctx->d_S + c0 || p->ldS != N || p->use_B || p->cur != 0;
+        p->cur = 0;
+        p->S64 = ctx->d_S + c0;
+        p->ldS = N;
+        p->use_B = false;
+        if (changed) rts_group_invalidate(s.chunk[i]);
+        if ((rc = rts_group_prepare(s.chunk[i], 0, st)) != RTS_OK) return rc;
+        rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode, p->rs,
+                                    p->rows_pad, p->a[0], st);
+        if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, st);
+        if (rc != RTS_OK) return rc;
+    }
+    return RTS_OK;
+}
+
 int rts_split_read(rts_ctx* ctx, double* S_host)
 {
     RTS_REQUIRE(ctx, ctx->split.iter, RTS_ERR_BAD_STATE, "no tensor-path source iteration set up");

@@ -1,0 +1,209 @@
+"""The device transport sweep against the oracle's restatement of the
+reference's sweep (Illum_async.cpp:726-783 with GetCurIllum, ReCalcIllum,
+BoundaryConditions) and of make_illum_struct / build_graph, through the C ABI.
+
+Tolerances: the per-direction structures match exactly (cell order, step
+boundaries, face states, in-faces) and the node distances to 1e-13 relative
+(FP64 geometry, fused multiply-adds on the device); Illum after FP64 sweeps
+and source iterations to 1e-12 relative (FP64 contract; the device exp
+differs from the host's by an ulp); iterations with the FP16x3 tensor-core
+scattering to 1e-6 relative (the split-precision contract)."""
+import numpy as np
+import pytest
+
+import oracle
+from relativistic_solver_hllc_gb300 import (
+    BOUND_OUTSOURCE,
+    LOCX0_DTYPE,
+    MEDIUM_ABSORPTION,
+    RtsError,
+    _native,
+    medium,
+    mesh_cube,
+)
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = np.maximum(np.abs(b), 1e-300)
+    mask = (np.abs(a) > 0) | (np.abs(b) > 0)
+    return float(np.max(np.abs(a - b)[mask] / den[mask])) if mask.any() else 0.0
+
+
+def setup(ctx, n, M, tilt=True, rule=1):
+    vert, pairs, normals = mesh_cube(n, rule, tilt)
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    N = vert.shape[0]
+    ctx.init(xyz, area, fa, N)
+    ctx.sweep_set_mesh(vert, pairs, normals)
+    return vert, pairs, normals, xyz, area, fa, N
+
+
+def coefficients(N, seed, kind):
+    rng = np.random.default_rng(seed)
+    if kind == "class1":
+        return np.full(N, 1.0), np.full(N, 0.5), np.full(N, 1.0)
+    if kind == "class10":
+        return np.full(N, 0.5), np.full(N, 100.0), np.zeros(N)
+    if kind == "thin":  # k s below 1e-3: the reference's own expression
+        return np.full(N, 2e-3), np.full(N, 1e-3), rng.uniform(0.0, 1.0, N)
+    return rng.uniform(0.5, 3.0, N), rng.uniform(0.0, 2.0, N), rng.uniform(0.0, 1.5, N)
+
+
+def same_norm(a, b, tol=TOL):
+    if np.isinf(a) or np.isinf(b):
+        return a == b
+    return abs(a - b) <= tol * max(1.0, abs(b))
+
+
+def test_structures_match_oracle(ctx):
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 4, 24)
+    rec, lev = ctx.sweep_build()
+    st = oracle.SweepStructures(vert, pairs, normals, xyz)
+    assert rec == st.s.shape[0]
+    assert lev == max(len(x) - 1 for x in st.levels)
+    for d in range(24):
+        order, states, recs = ctx.sweep_export_direction(d)
+        assert np.array_equal(order, st.order[d])
+        assert np.array_equal(states, st.states[d])
+        a, b = st.rec_off[d], st.rec_off[d + 1]
+        assert np.array_equal(recs["in_face_id"], st.face[a:b].astype(np.uint8))
+        assert rel_err(recs["s"], st.s[a:b]) <= 1e-13
+
+
+@pytest.mark.parametrize("kind,mode", [("class1", 0), ("class10", 0), ("random", 0), ("random", 1), ("ball", 0),
+                                       ("thin", 0)])
+def test_sweep_matches_oracle(ctx, kind, mode):
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 4, 40)
+    ctx.sweep_build()
+    st = oracle.SweepStructures(vert, pairs, normals, xyz)
+    a, b, q = coefficients(N, 5, "random" if kind == "ball" else kind)
+    if kind == "ball":
+        md = medium(0, ball=(0.5, 0.4, 0.5), radius=0.3, ball_coef=(0.5, 0.5, 2.0))
+    else:
+        md = medium(mode, s_scale=3.0 if mode == MEDIUM_ABSORPTION else 1.0)
+    bc = (0.0, 0.25, 1.0, 0.5)
+    ctx.sweep_set_medium(md, a, b, q, bc)
+    il0 = np.random.default_rng(9).uniform(0.1, 1.0, (40, N, 4))
+    # the sweep's source term is the device scattering array: fill it with the
+    # FP64 integral of il0 (which also leaves il0 as the device Illum) and
+    # hand the oracle the same numbers
+    S = ctx.scattering(il0.ravel()).reshape(40, N)
+    ref = il0.copy()
+    n_ref = oracle.sweep(st, S, a, b, q, ref, md=oracle.medium(md.mode, md.s_scale, md.i_scale, tuple(md.ball),
+                                                                md.radius, (md.ball_alpha, md.ball_beta, md.ball_q)),
+                         bc=bc)
+    n_dev = ctx.sweep()
+    got = np.empty(40 * N * 4)
+    ctx.read_illum(got)
+    assert rel_err(got, ref.ravel()) <= TOL, rel_err(got, ref.ravel())
+    assert same_norm(n_dev, n_ref), (n_dev, n_ref)
+
+
+def oracle_solve(st, xyz, area, fa, il, S, a, b, q, md, bc, iters, accuracy):
+    N, D = st.N, st.D
+    norms = []
+    for it in range(iters):
+        norms.append(oracle.sweep(st, S, a, b, q, il, md=md, bc=bc))
+        if iters > 1:
+            S = oracle.calculate_int_cpu(N, xyz, area, fa, il.ravel()).reshape(D, N)
+        if not norms[-1] > accuracy:
+            break
+    return np.array(norms), S
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL), ("fp16x3", 1e-6)])
+def test_illum_solve_matches_oracle(ctx, precision, tol):
+    M = 30
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 4, M)
+    ctx.sweep_build()
+    st = oracle.SweepStructures(vert, pairs, normals, xyz)
+    a, b, q = coefficients(N, 2, "class1")
+    bc = (0.0, 0.0, 1.0, 0.0)
+    ctx.sweep_set_medium(medium(), a, b, q, bc)
+    il = np.zeros((M, N, 4))
+    ctx.copy_illum(il.ravel())
+    norms = ctx.illum_solve(precision, max_iter=6, accuracy=1e-300)
+    ref_norms, _ = oracle_solve(st, xyz, area, fa, il, np.zeros((M, N)), a, b, q, oracle.medium(), bc, 6, 1e-300)
+    got = np.empty(M * N * 4)
+    ctx.read_illum(got)
+    assert len(norms) == len(ref_norms) == 6
+    assert rel_err(got, il.ravel()) <= tol, rel_err(got, il.ravel())
+    assert rel_err(norms[1:], ref_norms[1:]) <= 1e-9 if precision == "fp64" else True
+
+
+def test_illum_solve_stops_at_accuracy(ctx):
+    M = 16
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 3, M)
+    ctx.sweep_build()
+    a, b, q = coefficients(N, 2, "class1")
+    ctx.sweep_set_medium(medium(), a, b, q)
+    ctx.copy_illum(np.zeros(M * N * 4))
+    norms = ctx.illum_solve("fp64", max_iter=200, accuracy=1e-8)
+    assert norms[-1] <= 1e-8 and len(norms) < 200
+    assert np.all(norms[:-1] > 1e-8)
+
+
+def test_import_equals_build(ctx):
+    """The reference's file layouts (graph, state_face, LocX0) exported from
+    the built structures and imported again give the same sweep."""
+    M = 12
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 3, M)
+    ctx.sweep_build()
+    a, b, q = coefficients(N, 4, "random")
+    ctx.sweep_set_medium(medium(), a, b, q)
+    il0 = np.random.default_rng(3).uniform(0.1, 1.0, M * N * 4)
+    ctx.copy_illum(il0)
+    ctx.sweep()
+    built = np.empty(M * N * 4)
+    ctx.read_illum(built)
+    files = [ctx.sweep_export_direction(d) for d in range(M)]
+    # reverse each step's cells: still a valid dependency order
+    for d, (order, states, recs) in enumerate(files):
+        st = oracle.SweepStructures(vert, pairs, normals, xyz[d:d + 1])
+        rev = np.concatenate([order[st.levels[0][i]:st.levels[0][i + 1]][::-1] for i in range(len(st.levels[0]) - 1)])
+        # records follow the file's cell order
+        pos = {int(c): i for i, c in enumerate(order)}
+        nrec = 3 * (4 - np.array([bin(int(s)).count("1") for s in states]))
+        start = np.concatenate([[0], np.cumsum(nrec[order])])
+        recs2 = np.concatenate([recs[start[pos[int(c)]]:start[pos[int(c)] + 1]] for c in rev])
+        ctx.sweep_import_direction(d, rev, states, recs2)
+    ctx.copy_illum(il0)
+    ctx.sweep()
+    imported = np.empty(M * N * 4)
+    ctx.read_illum(imported)
+    assert np.array_equal(built, imported)
+
+
+def test_degenerate_direction_is_reported(ctx):
+    # the axis-aligned cube: the first Fibonacci direction (y = 0) runs along
+    # the y faces, where no in-face contains the back-traced node
+    setup(ctx, 3, 8, tilt=False)
+    with pytest.raises(RtsError) as e:
+        ctx.sweep_build()
+    assert e.value.status == _native.ERR_UNSUPPORTED
+
+
+def test_sweep_needs_structures_and_medium(ctx):
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 2, 4)
+    with pytest.raises(RtsError) as e:
+        ctx.sweep()
+    assert e.value.status == _native.ERR_BAD_STATE
+    ctx.sweep_build()
+    with pytest.raises(RtsError) as e:
+        ctx.sweep()
+    assert e.value.status == _native.ERR_BAD_STATE
+    bad = pairs.copy()
+    bad[0, 0] = 4 * N + 7
+    with pytest.raises(RtsError) as e:
+        ctx.sweep_set_mesh(vert, bad, normals)
+    assert e.value.status == _native.ERR_INVALID_ARGUMENT
+
+
+def test_boundary_codes_of_the_cube(ctx):
+    vert, pairs, normals = mesh_cube(3, 1, True)
+    assert (pairs == BOUND_OUTSOURCE).sum() == 2 * 9
+    assert LOCX0_DTYPE.itemsize == 32
