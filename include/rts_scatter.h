@@ -163,6 +163,13 @@ int rts_read_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, do
 int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
                           const double* B_host, double lambda, double* S_host);
 
+/* Copies rows [start, end) of a host scattering array (host + start*N) into
+ * the device scattering array on `stream`, the H2D counterpart of
+ * rts_read_scattering: the source term of the device sweep when the
+ * scattering comes from elsewhere (the reference's CPU sweep reads
+ * grid_t::scattering from host memory). */
+int rts_send_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, const double* host);
+
 /* Allocation-free FP64 scattering integral.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory --
  * code that runs inside a caller-owned memory pool or arena, code called
@@ -478,11 +485,11 @@ int rts_sweep_set_mesh(rts_ctx* ctx, const double* vert, const int32_t* pairs, c
 /* Builds the per-direction structures of the local directions on the
  * device, the work of make_illum_struct and build_graph: the in/out state of
  * every face (GetInAndOutFaces, utils/grid_geometry/geometry_solve.cpp:212-227),
- * the cells in dependency order (build_graph_calculation.cpp:347-513: steps
+ * the cells in dependency order (build_graph_calculation.cpp:347-510: steps
  * of cells whose in-faces are all known, each step in ascending cell id),
  * and for every out-face node (MakeArrayX) the in-face hit going back along
  * the direction and the distance to it (CalculateNodeValue,
- * struct_short_characteristics_logic_function.cpp:209-243).  *records (may
+ * struct_short_characteristics_logic_function.cpp:222-254).  *records (may
  * be NULL) receives the node count over all local directions, *levels the
  * largest number of steps of one direction.  RTS_ERR_UNSUPPORTED when a
  * direction's dependencies form a cycle or a node finds no in-face (a
@@ -515,8 +522,8 @@ int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const double* alpha
                          const double* Q, const double* bc);
 
 /* One sweep of every local direction (the direction loops of
- * MPI_CalculateIllumAsync, solve_module/illum/Illum_async.cpp:726-783 and
- * 831-885) on `stream`: reads the device scattering array [local][N] and
+ * MPI_CalculateIllumAsync, solve_module/illum/Illum_async.cpp:726-784 and
+ * 827-885) on `stream`: reads the device scattering array [local][N] and
  * writes the face means of the local directions' rows of the device Illum
  * (ReCalcIllum, :472-510).  *norm (may be NULL) receives ReCalcIllum's
  * max |old - new| / new over all faces (-1 if every term was NaN), which

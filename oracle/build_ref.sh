@@ -19,6 +19,23 @@
 #   Illum_async.cpp:1250-1349 IntegarteDirection9, MakeDivImpuls (impulse
 #                             tensor and its divergence)
 #   solve_utils.cpp:177-202   GetSend, GetDisp
+#
+# A second library, oracle/_ref/libref_sweep.so, holds the reference's
+# transport sweep and the structures it reads, with
+# oracle/ref_standin/sweep_standin.hpp in front and the harness of
+# sweep_entry_head.cpp / sweep_entry_tail.cpp around the sweep loop:
+#   make_illum_struct/struct_short_characteristics_calculations.cpp:102-118,
+#       124-128, 146-183  FromLocalToGlobalTetra, FromPlaneToTetra, BaseTetra_t
+#   utils/grid_geometry/geometry_solve.cpp:8-56, 109-159, 212-227
+#       SetBasis, Make2dPoint, IntersectionWithPlane, InTriangle, GetInAndOutFaces
+#   make_illum_struct/struct_short_characteristics_logic_function.cpp:10-73,
+#       222-297  MakeArrayX, CalculateNodeValue, GetNodes
+#   build_graph/build_graph_calculation.cpp:92-121, 347-391, 482-510
+#       FindInAndOutFaces, InitFacesState, FindNumberOfAllInnerFaceAndKnew,
+#       FindCurCell, NewStep
+#   solve_module/illum/illum_utils.cpp:407-474  BoundaryConditions
+#   solve_module/illum/Illum_async.cpp:172-199, 259-510, 726-784
+#       CalculateIllumeOnInnerFace, GetCurIllum, ReCalcIllum, the sweep loop
 set -eu
 REF=${RTS_REFERENCE_ROOT:-/root/reference}/solver_hllc_illum_cuda
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -48,3 +65,32 @@ UTL="$REF/solve_module/solve_utils.cpp"
     cat "$HERE/ref_standin/entry.cpp"
 } | g++ -x c++ -std=c++17 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w -o "$OUT/libref_scatter.so" -
 echo "built $OUT/libref_scatter.so"
+
+piece() {  # piece FILE FIRST LAST: the reference's lines FIRST..LAST, with their origin
+    echo "#line $2 \"$1\""
+    iconv -f cp1251 -t utf-8 "$REF/$1" | sed -n "$2,$3p"
+}
+{
+    cat "$HERE/ref_standin/sweep_standin.hpp"
+    piece make_illum_struct/struct_short_characteristics_calculations.cpp 102 118
+    piece make_illum_struct/struct_short_characteristics_calculations.cpp 124 128
+    piece make_illum_struct/struct_short_characteristics_calculations.cpp 146 183
+    echo 'static const BaseTetra_t base_tetra_geo;'
+    piece utils/grid_geometry/geometry_solve.cpp 8 56
+    piece utils/grid_geometry/geometry_solve.cpp 109 159
+    piece utils/grid_geometry/geometry_solve.cpp 212 227
+    piece make_illum_struct/struct_short_characteristics_logic_function.cpp 10 73
+    piece make_illum_struct/struct_short_characteristics_logic_function.cpp 222 297
+    piece build_graph/build_graph_calculation.cpp 92 121
+    piece build_graph/build_graph_calculation.cpp 347 391
+    piece build_graph/build_graph_calculation.cpp 482 510
+    piece solve_module/illum/illum_utils.cpp 407 474
+    piece solve_module/illum/Illum_async.cpp 172 199
+    piece solve_module/illum/Illum_async.cpp 259 510
+    echo '#line 1 "oracle/ref_standin/sweep_entry_head.cpp"'
+    cat "$HERE/ref_standin/sweep_entry_head.cpp"
+    piece solve_module/illum/Illum_async.cpp 726 784
+    echo '#line 1 "oracle/ref_standin/sweep_entry_tail.cpp"'
+    cat "$HERE/ref_standin/sweep_entry_tail.cpp"
+} | g++ -x c++ -std=c++14 -O2 -ffp-contract=off -fPIC -shared -w -o "$OUT/libref_sweep.so" -
+echo "built $OUT/libref_sweep.so"

@@ -11,19 +11,19 @@
  *                        cross product of the face's first two edges,
  *                        normalised, pointing away from the fourth vertex
  *   orc_sweep_nodes .... MakeArrayX (make_illum_struct/
- *                        struct_short_characteristics_logic_function.cpp:10-66)
+ *                        struct_short_characteristics_logic_function.cpp:10-73)
  *                        with FromLocalToGlobalTetra, FromPlaneToTetra and the
  *                        BaseTetra_t constants
- *                        (struct_short_characteristics_calculations.cpp:142-184)
+ *                        (struct_short_characteristics_calculations.cpp:102-128,146-183)
  *   face states ........ GetInAndOutFaces (utils/grid_geometry/geometry_solve.cpp:212-227)
  *   orc_sweep_graph .... build_graph's cell order: FindNumberOfAllInnerFaceAndKnew,
  *                        FindCurCell, NewStep (build_graph/build_graph_calculation.cpp:
- *                        347-391,482-513) driven as in build_graph/build_graph_main.cpp:165-300
- *   orc_sweep_x0 ....... GetNodes / CalculateNodeValue (logic_function.cpp:209-297)
+ *                        347-391,482-510) driven as in build_graph/build_graph_main.cpp:165-300
+ *   orc_sweep_x0 ....... GetNodes / CalculateNodeValue (logic_function.cpp:222-297)
  *                        with IntersectionWithPlane, InTriangle, SetBasis,
  *                        Make2dPoint (geometry_solve.cpp:8-56,109-159)
  *   orc_sweep_dir ...... one direction of the sweep in MPI_CalculateIllumAsync
- *                        (solve_module/illum/Illum_async.cpp:726-783) with
+ *                        (solve_module/illum/Illum_async.cpp:726-784) with
  *                        CalculateIllumeOnInnerFace (:172-199), GetCurIllum
  *                        (:259-470, as a parametrised medium), ReCalcIllum
  *                        (:472-510) and BoundaryConditions
@@ -47,8 +47,8 @@
  * ReCalcIllum, BoundaryConditions, CalculateIllumeOnInnerFace, the sweep loop
  * body and the geometry functions from the reference source text (development
  * container only); tests/golden/make_golden.py ran them on small cube meshes
- * and tests/test_sweep_oracle.py checks this restatement against the stored
- * outputs.
+ * and tests/test_sweep_golden.py checks this restatement against the stored
+ * outputs (bit for bit).
  */
 #include <math.h>
 #include <stdint.h>

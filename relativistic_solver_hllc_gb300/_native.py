@@ -88,6 +88,7 @@ _SIGNATURES = {
     "rts_scattering": (C.c_int, [_vp, _dp, _dp]),
     "rts_read_scattering": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
     "rts_scattering_update": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_double, _dp]),
+    "rts_send_scattering": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
     "rts_device_arrays": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
     "rts_moments": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "rts_set_geometry": (C.c_int, [_vp, _dp, _dp, _dp]),
@@ -488,6 +489,14 @@ class Context:
             self._keep.append(out)
         self._check(self.lib.rts_read_scattering(self.h, int(start), int(end), int(stream), _ptr(out)),
                     "rts_read_scattering")
+
+    def send_scattering(self, S, start: int = 0, end: int | None = None, stream: int = STREAM_SCATTERING_1):
+        """Rows [start, end) of S ([local][N] FP64, host) into the device scattering array (synchronous)."""
+        end = (self.end - self.start) if end is None else end
+        a = _f64(S, ((self.end - self.start) * self.N,))
+        self._check(self.lib.rts_send_scattering(self.h, int(start), int(end), int(stream), _ptr(a)),
+                    "rts_send_scattering")
+        self.sync_stream(stream)
 
     def device_arrays(self):
         a, b = _dp(), _dp()

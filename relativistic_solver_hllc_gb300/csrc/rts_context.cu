@@ -489,6 +489,23 @@ int rts_read_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, do
     return RTS_OK;
 }
 
+int rts_send_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, const double* host)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_REQUIRE(ctx, ctx->d_S, RTS_ERR_BAD_STATE, "rts_send_scattering before rts_init");
+    RTS_REQUIRE(ctx, valid_stream(stream), RTS_ERR_INVALID_ARGUMENT, "bad stream id %d", stream);
+    RTS_REQUIRE(ctx, host, RTS_ERR_INVALID_ARGUMENT, "rts_send_scattering: null host array");
+    RTS_REQUIRE(ctx, 0 <= start && start <= end && end <= ctx->local(), RTS_ERR_INVALID_ARGUMENT,
+                "rts_send_scattering: [%lld,%lld) outside the %lld local out-directions", (long long)start,
+                (long long)end, (long long)ctx->local());
+    if (start == end) return RTS_OK;
+    ctx->solve_ready = false;
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_S + start * ctx->N, host + start * ctx->N,
+                                      rts_bytes<double>((end - start) * ctx->N), cudaMemcpyHostToDevice,
+                                      ctx->streams[stream]));
+    return RTS_OK;
+}
+
 int rts_device_arrays(rts_ctx* ctx, double** d_illum, double** d_scattering)
 {
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;

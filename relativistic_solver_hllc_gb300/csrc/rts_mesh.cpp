@@ -64,11 +64,11 @@ void rts_face_normals_host(int64_t N, const double* vert, double* normals)
 }
 
 // MakeArrayX (make_illum_struct/struct_short_characteristics_logic_function.cpp:
-// 10-66): the 3 nodes of face f sit at the local coordinates of the rows of
+// 10-73): the 3 nodes of face f sit at the local coordinates of the rows of
 // straight_face ({1/6,1/6}, {2/3,1/6}, {1/6,2/3}) on the coordinate plane the
 // face lies in, or for face 3 at the rows of inclined_face carried from the
 // inclined plane by inverse_transform_matrix and start_point_plane_coord
-// (struct_short_characteristics_calculations.cpp:142-184); local coordinates
+// (struct_short_characteristics_calculations.cpp:102-128,146-183); local coordinates
 // xi map to sum_j V_j xi_j + V_3 (1 - xi_0 - xi_1 - xi_2) (FromLocalToGlobalTetra).
 void rts_sweep_nodes_host(int64_t N, const double* vert, double* nodes)
 {

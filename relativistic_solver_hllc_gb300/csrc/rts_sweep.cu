@@ -1,7 +1,7 @@
 // rts_sweep.cu -- the transport sweep that produces Illum, on the device.
 //
 // For every direction the reference walks the cells in dependency order
-// (Illum_async.cpp:726-783): at each out-face node it takes the mean of the
+// (Illum_async.cpp:726-784): at each out-face node it takes the mean of the
 // in-face the characteristic comes from, integrates GetCurIllum over the
 // distance s to it, and stores the three node values of the face for the
 // face and its neighbour's copy; ReCalcIllum then writes the face means into
@@ -114,7 +114,7 @@ struct X0Args {
 };
 
 // CalculateNodeValue (make_illum_struct/struct_short_characteristics_logic_function.cpp:
-// 209-243) for the 3 nodes of every item: the first in-face, in face order,
+// 222-254) for the 3 nodes of every item: the first in-face, in face order,
 // whose triangle contains the back-traced point, and the distance to it.
 // Grid: x over the items of a direction, y over the directions.
 __global__ void __launch_bounds__(256) sweep_x0_kernel(X0Args a)
@@ -348,7 +348,7 @@ int popcount4(int x) { return (x & 1) + ((x >> 1) & 1) + ((x >> 2) & 1) + ((x >>
 // Dependency order of one direction: steps of cells whose in-faces all have
 // known values (boundary faces are known from the start), each step in
 // ascending cell id -- the order build_graph writes (build_graph/
-// build_graph_calculation.cpp:347-391,482-513, driven by build_graph_main.cpp:
+// build_graph_calculation.cpp:347-391,482-510, driven by build_graph_main.cpp:
 // 165-300).  A cell enters the step after the last of its upstream cells.
 // lev receives the cell offset of every step and the end.  Returns false on
 // a dependency cycle.
