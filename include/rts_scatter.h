@@ -587,6 +587,11 @@ int rts_autotune_load(rts_ctx* ctx, const char* path);
  * or record CUDA events against the library's streams). */
 int rts_stream_handle(rts_ctx* ctx, int stream, void** handle);
 
+/* Self-check of the sweep's FP64 exponential (a table-driven method for
+ * arguments in [-700, 0]) against CUDA's exp at n points of that range:
+ * *max_ulp receives the largest difference in units in the last place. */
+int rts_sweep_exp_check(rts_ctx* ctx, int64_t n, double* max_ulp);
+
 /* Number of kernels this context has launched so far. */
 int rts_launch_count(const rts_ctx* ctx, int64_t* count);
 

@@ -128,6 +128,7 @@ _SIGNATURES = {
     "rts_sweep_export_direction": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _i64, C.POINTER(_i64)]),
     "rts_sweep_set_medium": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _dp]),
     "rts_sweep": (C.c_int, [_vp, C.c_int, _dp]),
+    "rts_sweep_exp_check": (C.c_int, [_vp, _i64, _dp]),
     "rts_illum_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.POINTER(_i64), _dp]),
 }
 
@@ -660,6 +661,11 @@ class Context:
         out = C.c_double(0.0)
         self._check(self.lib.rts_sweep(self.h, int(stream), C.byref(out) if read_norm else None), "rts_sweep")
         return out.value if read_norm else None
+
+    def sweep_exp_check(self, n: int = 1 << 20) -> float:
+        out = C.c_double()
+        self._check(self.lib.rts_sweep_exp_check(self.h, int(n), C.byref(out)), "rts_sweep_exp_check")
+        return out.value
 
     def illum_solve(self, precision="fp64", max_iter: int = 1, accuracy: float = 1e-5):
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)

@@ -35,6 +35,9 @@ void rts_sweep_nodes_host(int64_t N, const double* vert, double* nodes);
 
 namespace {
 
+// 128 threads and at most 72 registers: 7 CTAs per SM, so one wave of 152 x 7
+// CTAs holds 1000 directions (the sweep is bound by the FP64 pipe; a second
+// partial wave cost 11 %).
 constexpr int SWEEP_THREADS = 128;
 constexpr double SWEEP_EPS = 1e-10;  // `eps`, global_value.h:13
 
@@ -169,67 +172,103 @@ struct SweepArgs {
     const int32_t* nbnd;     // [D]
     const int32_t* pairs;    // [N][4]
     const double* nodes;     // [N][4][3][3] (read only with a ball)
-    const double* med;       // [N][4] alpha, beta, Q
+    const double* med;       // [N][4] alpha, beta, Q, 1/k
     const double* S;         // [D][N]
     double* illum;           // [D][N][4], rows of the local directions
     int64_t N;
     rts_medium md;
     double bc[4];
+    double exp2tab[32];      // 2^(j/32)
+    double ball_inv_k;       // 1 / k of the ball's coefficients
     unsigned long long* norm;
 };
 
+// exp(x) for -700 <= x <= 0 by Tang's table-driven method (P. T. P. Tang,
+// "Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (32 m + j) ln2/32 + r
+// with |r| <= ln2/64, exp(x) = 2^m 2^(j/32) (1 + p(r)), p the degree-6 Taylor
+// polynomial of exp(r) - 1 (truncation below 4e-18), 2^(j/32) from a 32-entry
+// table and 2^m added to the exponent field.  11 FP64 operations against the
+// general exp's range checks and longer polynomial; within 1 ulp of the exact
+// value over the range (checked against CUDA's exp by rts_sweep_exp_check).
+constexpr double kExpInvL = 46.16624130844683;            // 32 / ln 2
+constexpr double kExpLHi = 0.02166084939249829;           // ln 2 / 32, leading part
+constexpr double kExpLLo = 7.247021293269686e-19;         // ln 2 / 32 - kExpLHi
+constexpr double kExpShift = 6755399441055744.0;          // 1.5 * 2^52: rounds to an integer
+
+__device__ __forceinline__ double exp_neg(double x, const double* __restrict__ tab)
+{
+    const double t = fma(x, kExpInvL, kExpShift);
+    const int n = __double2loint(t);
+    const double N = t - kExpShift;
+    double r = fma(-N, kExpLHi, x);
+    r = fma(-N, kExpLLo, r);
+    double h = fma(r, 1.0 / 720, 1.0 / 120);
+    h = fma(r, h, 1.0 / 24);
+    h = fma(r, h, 1.0 / 6);
+    h = fma(r, h, 0.5);
+    const double p = fma(r * r, h, r);
+    const double T = tab[n & 31];
+    const double y = fma(T, p, T);
+    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> 5) << 52));
+}
+
 // Per-cell terms of GetCurIllum (solve_module/illum/Illum_async.cpp:259-470):
-// scattering form k = alpha + beta, R = Q + S' beta, Rk = R / k; absorption
-// form k = alpha, R = Q, Rk = Q / alpha.
+// scattering form k = alpha + beta, R = Q + S' beta; absorption form
+// k = alpha, R = Q; ks = k * s_scale, Rk = R / k (from the medium table's
+// 1 / k, kept per cell so that no node divides).
 struct CellTerms {
-    double k, R, Rk;
+    double k, ks, R, Rk;
 };
 
-__device__ inline CellTerms cell_terms(const rts_medium& md, double alpha, double betta, double Q, double S)
+__device__ inline CellTerms cell_terms(const rts_medium& md, double alpha, double betta, double Q, double inv_k,
+                                       double S)
 {
     CellTerms t;
     if (md.mode == RTS_MEDIUM_ABSORPTION) {
-        t.k = alpha, t.R = Q, t.Rk = Q / alpha;
+        t.k = alpha;
+        t.R = Q;
     } else {
         t.k = alpha + betta;
-        t.R = Q + S * md.i_scale * betta;
-        t.Rk = t.R / t.k;
+        t.R = Q + (md.i_scale == 1.0 ? S : S * md.i_scale) * betta;
     }
+    t.ks = md.s_scale == 1.0 ? t.k : t.k * md.s_scale;
+    t.Rk = t.R * inv_k;
     return t;
 }
 
-// GetCurIllum for one node at distance s from the in-face value I_0.  The
-// reference evaluates exp(-x) (I0 k + (exp(x) - 1) R) / k, x = k s; where
-// 1e-3 <= x <= 700 this is evaluated as e I0 + (1 - e) R / k with e = exp(-x)
-// -- the same number up to a few ulp (both lose ~eps / x to the cancellation
-// in exp(x) - 1, resp. 1 - e) for one exponential and no division per node,
-// the dominant FP64 cost.  Outside that range the reference's own expression
-// runs (including its overflow past x = 709).
-__device__ inline double node_illum(const rts_medium& md, const CellTerms& t, double s, double I_0)
+// The reference's own expressions, for the nodes outside the fast path
+// (kept out of line: they are rare and their exponentials cost registers).
+__device__ __noinline__ double node_illum_ref(int mode, double k, double ss, double I0, double R)
 {
-    const double ss = s * md.s_scale;
-    double I;
-    if (md.mode == RTS_MEDIUM_ABSORPTION) {
-        if (t.k > 1e-15) {
-            const double e = exp(-t.k * ss);
-            I = I_0 * e + (1 - e) * t.Rk;
-        } else {
-            I = I_0 * (1 - t.k * ss) + t.R * ss;
-        }
-        return I < 0 ? 0.0 : I;
+    if (mode == RTS_MEDIUM_ABSORPTION) {
+        if (k > 1e-15) return I0 * exp(-k * ss) + R * (1 - exp(-k * ss)) / k;
+        return I0 * (1 - k * ss) + R * ss;
     }
+    if (k > 1e-10) return (exp(-k * ss) * (I0 * k + (exp(k * ss) - 1) * R)) / k;
+    return (1 - ss * k) * (I0 + ss * R);
+}
+
+// GetCurIllum for one node at distance s from the in-face value I_0.  The
+// reference evaluates exp(-x) (I0 k + (exp(x) - 1) R) / k, x = k s (the
+// scattering form) or I0 exp(-x) + R (1 - exp(-x)) / k (the absorption
+// form); where 1e-3 <= x <= 700 both are evaluated as e I0 + (1 - e) R / k
+// with e = exp(-x) -- the same number up to a few ulp (the reference and this
+// form both lose ~eps / x to the cancellation in exp(x) - 1, resp. 1 - e) for
+// one exponential and no division per node, the dominant FP64 cost.  Outside
+// that range the reference's own expression runs (including its overflow
+// past x = 709).
+__device__ inline double node_illum(const rts_medium& md, const CellTerms& t, double s, double I_0,
+                                    const double* __restrict__ tab)
+{
+    const double x = t.ks * s;
     const double I0 = md.i_scale == 1.0 ? I_0 : I_0 * md.i_scale;
-    const double k = t.k;
-    if (k > 1e-10) {
-        const double x = k * ss;
-        if (x >= 1e-3 && x <= 700.0) {
-            const double e = exp(-x);
-            I = e * I0 + (1 - e) * t.Rk;
-        } else {
-            I = (exp(-x) * (I0 * k + (exp(x) - 1) * t.R)) / k;
-        }
+    double I;
+    if (x >= 1e-3 && x <= 700.0) {
+        const double e = exp_neg(-x, tab);
+        I = e * I0 + (1 - e) * t.Rk;
     } else {
-        I = (1 - ss * k) * (I0 + ss * t.R);
+        I = node_illum_ref(md.mode, t.k, md.s_scale == 1.0 ? s : s * md.s_scale, I0, t.R);
     }
     if (I < 0) return 0.0;
     return md.i_scale == 1.0 ? I : I / md.i_scale;
@@ -263,7 +302,7 @@ __device__ inline int pick(int g, int v0, int v1, int v2, int v3)
 // (visible after the barrier); it writes its mean to the face and to the
 // neighbour's copy.  Every face is written once per sweep, so each writer
 // takes ReCalcIllum's term against the old value.
-__global__ void __launch_bounds__(SWEEP_THREADS) sweep_kernel(SweepArgs a)
+__global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
 {
     const int64_t d = blockIdx.x;
     const int64_t N = a.N;
@@ -274,6 +313,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS) sweep_kernel(SweepArgs a)
     const double* Sd = a.S + d * N;
     double* Il = a.illum + d * N * 4;
     const bool ball = a.md.radius > 0;
+    __shared__ double tab[32];
+    if (threadIdx.x < 32) tab[threadIdx.x] = a.exp2tab[threadIdx.x];
+    __syncthreads();
     double loc = -1.0;
     {
         const uint32_t* bnd = a.bnd[d];
@@ -296,9 +338,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS) sweep_kernel(SweepArgs a)
             const double2 f23 = *reinterpret_cast<const double2*>(Il + 4 * c + 2);
             const int4 pr = *reinterpret_cast<const int4*>(a.pairs + 4 * c);
             const double2 m01 = *reinterpret_cast<const double2*>(a.med + 4 * c);
-            const double Qc = a.med[4 * c + 2];
+            const double2 m23 = *reinterpret_cast<const double2*>(a.med + 4 * c + 2);
             const double Sc = Sd[c];
-            const CellTerms cell = cell_terms(a.md, m01.x, m01.y, Qc, Sc);
+            const CellTerms cell = cell_terms(a.md, m01.x, m01.y, m23.x, m23.y, Sc);
             const double* sr = recs + 3 * (int64_t)i;
             double I[3];
 #pragma unroll
@@ -312,9 +354,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS) sweep_kernel(SweepArgs a)
                     const double* x = a.nodes + 36 * c + 9 * f + 3 * m;
                     const double d0 = x[0] - a.md.ball[0], d1 = x[1] - a.md.ball[1], d2 = x[2] - a.md.ball[2];
                     if (sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius)
-                        t = cell_terms(a.md, a.md.ball_alpha, a.md.ball_beta, a.md.ball_q, Sc);
+                        t = cell_terms(a.md, a.md.ball_alpha, a.md.ball_beta, a.md.ball_q, a.ball_inv_k, Sc);
                 }
-                I[m] = node_illum(a.md, t, sr[m], I_x0);
+                I[m] = node_illum(a.md, t, sr[m], I_x0, tab);
             }
             const double mean = (I[0] + I[1] + I[2]) * (1.0 / 3.0);
             norm_term(pick(f, f01.x, f01.y, f23.x, f23.y), mean, loc);
@@ -342,6 +384,38 @@ __global__ void __launch_bounds__(SWEEP_THREADS) sweep_kernel(SweepArgs a)
 }
 
 // ---------------------------------------------------------------- host side
+
+// 1 / k of GetCurIllum's coefficients (0 where k is 0: those nodes take the
+// reference's expression)
+double medium_inv_k(const rts_medium& md, double alpha, double betta)
+{
+    const double k = md.mode == RTS_MEDIUM_ABSORPTION ? alpha : alpha + betta;
+    return k != 0.0 ? 1.0 / k : 0.0;
+}
+
+void exp2_table(double* tab)
+{
+    for (int j = 0; j < 32; ++j) tab[j] = exp2((double)j / 32.0);
+}
+
+// exp_neg against CUDA's exp at n points spread over [-700, 0] (and the 1e-3
+// end): the largest difference in units in the last place of CUDA's value.
+__global__ void exp_check_kernel(int64_t n, const double* __restrict__ tab_in, double* out)
+{
+    __shared__ double tab[32];
+    if (threadIdx.x < 32) tab[threadIdx.x] = tab_in[threadIdx.x];
+    __syncthreads();
+    double worst = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double u = (double)i / (double)(n - 1);
+        const double x = i & 1 ? -700.0 * u : -1e-3 - u * u;  // the whole range, and densely near 0
+        const double a = exp_neg(x, tab), b = exp(x);
+        const double ulp = fabs(__longlong_as_double(__double_as_longlong(b) + 1) - b);
+        worst = fmax(worst, fabs(a - b) / ulp);
+    }
+    for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong(worst));
+}
 
 int popcount4(int x) { return (x & 1) + ((x >> 1) & 1) + ((x >> 2) & 1) + ((x >> 3) & 1); }
 
@@ -828,7 +902,7 @@ extern "C" int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const do
         m[4 * c] = alpha[c];
         m[4 * c + 1] = beta[c];
         m[4 * c + 2] = Q[c];
-        m[4 * c + 3] = 0.0;
+        m[4 * c + 3] = medium_inv_k(*md, alpha[c], beta[c]);
     }
     RTS_CUDA_TRY(ctx, cudaMemcpy(sw.d_med, m.data(), rts_bytes<double>(4 * N), cudaMemcpyHostToDevice));
     sw.md = *md;
@@ -859,6 +933,8 @@ static int enqueue_sweep(rts_ctx* ctx, cudaStream_t st)
     a.N = sw.N;
     a.md = sw.md;
     for (int i = 0; i < 4; ++i) a.bc[i] = sw.bc[i];
+    exp2_table(a.exp2tab);
+    a.ball_inv_k = medium_inv_k(sw.md, sw.md.ball_alpha, sw.md.ball_beta);
     a.norm = sw.d_norm;
     if (sw.D > 0) {
         rts_timing_begin(ctx, st);
@@ -941,5 +1017,30 @@ extern "C" int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double
         RTS_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
         if (flag) return rts_fail(ctx, RTS_ERR_DEVICE_WAIT, "tensor-path kernel reported device flag %d", flag);
     }
+    return RTS_OK;
+}
+
+extern "C" int rts_sweep_exp_check(rts_ctx* ctx, int64_t n, double* max_ulp)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_REQUIRE(ctx, n >= 2 && max_ulp, RTS_ERR_INVALID_ARGUMENT, "rts_sweep_exp_check: n >= 2 and an output");
+    double tab[32];
+    exp2_table(tab);
+    void* p = nullptr;
+    int rc = rts_dmalloc(ctx, &p, 33 * sizeof(double), "exp check");
+    if (rc != RTS_OK) return rc;
+    double* d = (double*)p;
+    cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
+    cudaError_t e = cudaMemcpyAsync(d, tab, 32 * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + 32, 0, sizeof(double), st);
+    if (e == cudaSuccess) {
+        exp_check_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(n, d, d + 32);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(max_ulp, d + 32, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    rts_dfree(ctx, d, 33 * sizeof(double));
+    if (e != cudaSuccess) return rts_fail(ctx, RTS_ERR_CUDA, "rts_sweep_exp_check: %s", cudaGetErrorString(e));
+    ctx->launches++;
     return RTS_OK;
 }

@@ -207,3 +207,9 @@ def test_boundary_codes_of_the_cube(ctx):
     vert, pairs, normals = mesh_cube(3, 1, True)
     assert (pairs == BOUND_OUTSOURCE).sum() == 2 * 9
     assert LOCX0_DTYPE.itemsize == 32
+
+
+def test_sweep_exponential_within_two_ulp_of_cuda(ctx):
+    """The sweep's table-driven exp against CUDA's exp over [-700, 0]: each is
+    within about an ulp of the exact value, so they differ by at most 2."""
+    assert ctx.sweep_exp_check(1 << 22) <= 2.0
