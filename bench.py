@@ -66,6 +66,9 @@ def parse():
                          "still meets the 1e-6 gate on this workload, checked in the same run)")
     ap.add_argument("--moments", action="store_true",
                     help="time the FP64 moment kernels on the config 2 Illum instead (one JSON line)")
+    ap.add_argument("--sweep", action="store_true",
+                    help="the transport sweep producing Illum (mesh n^3 x 6 tetrahedra, --dirs directions)")
+    ap.add_argument("--sweep-n", type=int, default=48, help="hexahedra per cube edge of the sweep's mesh")
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5],
                     help="2: the headline source iteration (default); 1, 3, 4, 5: the other configurations")
     return ap.parse_args()
@@ -151,6 +154,158 @@ def run_moments(args, rank, world, local):
                          "hbm_gbs": m["hbm_gbs"], "hbm_frac": m["hbm_gbs"] / hbm,
                          "peak_source": f"nominal GB300 FP64; HBM {src}"},
             "result": res, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def sweep_medium(N: int, seed: int = 11):
+    """Per-cell GetCurIllum coefficients of the sweep workload (scattering
+    form): alpha ~ U(0.5, 2), beta ~ U(0, 1), Q ~ U(0, 1), seeded."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(0.5, 2.0, N), rng.uniform(0.0, 1.0, N), rng.uniform(0.0, 1.0, N)
+
+
+def read_sweep_profile():
+    """FP64 operations per cell-direction of sweep_kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "sweep_fp64.json"
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return {}
+
+
+def run_sweep(args, rank, world, local):
+    """The transport sweep that produces Illum (one CTA per direction over
+    the dependency steps of the mesh): one JSON line.  Mesh: the unit cube,
+    n^3 hexahedra x 6 tetrahedra, turned by the fixed tilt (no face parallel
+    to a Fibonacci direction), boundary rule 1 (x = 0 side a source); --dirs
+    Fibonacci directions; seeded per-cell coefficients; the source term is the
+    FP64 scattering integral of the lognormal(0, 1.5) Illum."""
+    import torch
+
+    import relativistic_solver_hllc_gb300 as pkg
+    from relativistic_solver_hllc_gb300 import _native
+
+    pkg.build_library()
+    torch.cuda.set_device(local)
+    n, M, K, W = args.sweep_n, args.dirs, args.steps, args.warmup
+    vert, pairs, normals = pkg.mesh_cube(n, 1, True)
+    N = vert.shape[0]
+    xyz, area, fa = _native.synth_directions(M)
+    ctx = pkg.Context(local)
+    ctx.init(xyz, area, fa, N)
+    t0 = time.perf_counter()
+    ctx.sweep_set_mesh(vert, pairs, normals)
+    records, steps_max = ctx.sweep_build()
+    t_build = time.perf_counter() - t0
+    a, b, q = sweep_medium(N)
+    ctx.sweep_set_medium(pkg.medium(), a, b, q)
+    ctx.synth_illum(WORKLOAD["seed"], WORKLOAD["mu"], WORKLOAD["sigma"])
+    ctx.scattering_async(0, M, pkg.STREAM_SCATTERING_1)
+    ctx.sync_stream(pkg.STREAM_SCATTERING_1)
+    for _ in range(W):
+        ctx.sweep(read_norm=False)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    ctx.kernel_timing(True)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        ctx.sweep(read_norm=False)
+    norm = ctx.sweep()  # one more, read back: the timed region ends synchronised
+    elapsed = time.perf_counter() - t0
+    kern_ms, kern_n = ctx.kernel_timing(False)
+    launches = ctx.launch_count() - launches0
+    clk = clocks.stop()
+    kern_avg = kern_ms / max(kern_n, 1)
+    value = N * M / (kern_avg / 1e3) / 1e9
+
+    # parity spot check on two full-size directions against the oracle
+    accuracy = None
+    if rank == 0 and args.check != "none":
+        import oracle
+
+        oracle.build()
+        before = np.empty(M * N * 4)
+        ctx.read_illum(before)
+        S = np.empty(M * N)
+        ctx.read_scattering(0, M, pkg.STREAM_SCATTERING_1, S)
+        ctx.sync_stream(pkg.STREAM_SCATTERING_1)
+        S = S.reshape(M, N)
+        ctx.sweep()
+        after = np.empty(M * N * 4)
+        ctx.read_illum(after)
+        worst = 0.0
+        for d in (0, M // 2):
+            st = oracle.SweepStructures(vert, pairs, normals, xyz[d:d + 1])
+            il = before.reshape(M, N, 4)[d:d + 1].copy()
+            oracle.sweep(st, S[d:d + 1], a, b, q, il)
+            got = after.reshape(M, N, 4)[d:d + 1]
+            den = np.maximum(np.abs(il), 1e-300)
+            worst = max(worst, float(np.max(np.abs(got - il) / den)))
+        accuracy = {"vs": "oracle sweep (restated reference, FP64)", "directions": [0, M // 2],
+                    "max_rel_err": worst, "tolerance": 1e-11}
+
+    # end to end: the device source iteration (sweep + FP16x3 scattering per
+    # iteration, the norm read back each time) through rts_illum_solve
+    Ke = args.e2e_steps if args.e2e_steps is not None else max(3, K // 4)
+    ctx.illum_solve("fp16x3", max_iter=1 + 1, accuracy=0.0)  # warm-up of the split operands
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    norms = ctx.illum_solve("fp16x3", max_iter=Ke, accuracy=0.0)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": N * M * len(norms) / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": 8, "steps": len(norms),
+           "call": "rts_illum_solve (sweep + FP16x3 scattering per iteration, device-resident Illum and S, "
+                   "the 8-byte norm read back each iteration)"}
+
+    prof = read_sweep_profile()
+    fl = prof.get("fp64_flops_per_cell_dir")
+    achieved = fl * value * 1e9 / 1e12 if fl else None
+    roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+            "frac": achieved / FP64_NOMINAL_TFLOPS if achieved else None,
+            "traffic": prof.get("dram_bytes_per_cell_dir") and prof["dram_bytes_per_cell_dir"] * N * M,
+            "peak_source": "nominal GB300 FP64 (no measured FP64 peak available)",
+            "fp64_pipe_active": prof.get("fp64_pipe_active_frac"),
+            "note": "achieved = FP64 operations per cell-direction counted by ncu (dadd + dmul + 2 dfma) x the "
+                    "measured cell-direction rate",
+            "kernel_ms_avg": kern_avg, "kernel_launches_timed": kern_n}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        oracle.build()
+        nthr = oracle.max_threads()
+        Ds = max(1, nthr)
+        st = oracle.SweepStructures(vert, pairs, normals, xyz[:Ds])
+        S = np.empty(M * N)
+        ctx.read_scattering(0, Ds, pkg.STREAM_SCATTERING_1, S)
+        ctx.sync_stream(pkg.STREAM_SCATTERING_1)
+        S = S[:Ds * N].reshape(Ds, N)
+        il = np.random.default_rng(5).uniform(0.1, 1.0, (Ds, N, 4))
+        t0 = time.perf_counter()
+        oracle.sweep(st, S, a, b, q, il, nthreads=nthr)
+        dt = time.perf_counter() - t0
+        cpu = {"value": N * Ds / dt / 1e9, "unit": UNIT, "cores": nthr, "kind": "port",
+               "sample": f"the oracle sweep (restated Illum_async.cpp:726-784, GetCurIllum, ReCalcIllum; "
+                         f"bit-identical to the reference's own code on the golden cases) over directions "
+                         f"[0,{Ds}) of the full {N}-cell mesh, one direction per thread"}
+
+    line = {
+        "metric": "Transport sweep Gcell·dir/s (FP64, all directions of the mesh)", "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": kern_avg, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"transport sweep: unit cube {n}^3 x 6 = {N} tetrahedra (tilted), {M} Fibonacci "
+                               f"directions, alpha~U(0.5,2) beta~U(0,1) Q~U(0,1), boundary x=0 source",
+                   "cells": N, "dirs": M, "node_records": records, "max_steps": steps_max,
+                   "structures_build_s": t_build, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (no flush)", "step": "one sweep of every direction"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "accuracy": accuracy, "norm": norm, "wall_ms_per_step": elapsed / (K + 1) * 1e3,
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -497,6 +652,8 @@ def main():
         run_reference(args, rank)
     elif args.moments:
         run_moments(args, rank, world, local)
+    elif args.sweep:
+        run_sweep(args, rank, world, local)
     elif args.config != 2:
         run_other_config(args, rank, world, local)
     else:
