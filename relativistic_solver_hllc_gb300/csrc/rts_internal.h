@@ -94,7 +94,7 @@ struct rts_sweep_state {
     std::vector<int64_t> h_nitems;
     std::vector<std::pair<void*, size_t>> blocks;  // allocations behind the tables
     std::vector<char> have;          // direction d built or imported
-    double* d_med = nullptr;         // [N][4] alpha, beta, Q, 1/k
+    double* d_med = nullptr;         // [N][4] k, beta, Q, 1/k (k = alpha + beta, or alpha)
     rts_medium md{};
     double bc[4] = {0.0, 0.0, 1.0, 0.0};
     bool has_medium = false;

@@ -172,14 +172,14 @@ struct SweepArgs {
     const int32_t* nbnd;     // [D]
     const int32_t* pairs;    // [N][4]
     const double* nodes;     // [N][4][3][3] (read only with a ball)
-    const double* med;       // [N][4] alpha, beta, Q, 1/k
+    const double* med;       // [N][4] k, beta, Q, 1/k
     const double* S;         // [D][N]
     double* illum;           // [D][N][4], rows of the local directions
     int64_t N;
     rts_medium md;
     double bc[4];
     double exp2tab[32];      // 2^(j/32)
-    double ball_inv_k;       // 1 / k of the ball's coefficients
+    double ball[4];          // medium table entry of the ball's coefficients
     unsigned long long* norm;
 };
 
@@ -215,26 +215,32 @@ __device__ __forceinline__ double exp_neg(double x, const double* __restrict__ t
 
 // Per-cell terms of GetCurIllum (solve_module/illum/Illum_async.cpp:259-470):
 // scattering form k = alpha + beta, R = Q + S' beta; absorption form
-// k = alpha, R = Q; ks = k * s_scale, Rk = R / k (from the medium table's
-// 1 / k, kept per cell so that no node divides).
+// k = alpha, R = Q; ks = k * s_scale, Rk = R / k.  The medium table keeps k,
+// beta (0 in the absorption form), Q and 1 / k per cell, so that neither an
+// item nor a node adds or divides for them.
 struct CellTerms {
     double k, ks, R, Rk;
 };
 
-__device__ inline CellTerms cell_terms(const rts_medium& md, double alpha, double betta, double Q, double inv_k,
-                                       double S)
+__device__ inline CellTerms cell_terms(const rts_medium& md, bool unit_i, bool unit_s, double k, double betta,
+                                       double Q, double inv_k, double S)
 {
     CellTerms t;
-    if (md.mode == RTS_MEDIUM_ABSORPTION) {
-        t.k = alpha;
-        t.R = Q;
-    } else {
-        t.k = alpha + betta;
-        t.R = Q + (md.i_scale == 1.0 ? S : S * md.i_scale) * betta;
-    }
-    t.ks = md.s_scale == 1.0 ? t.k : t.k * md.s_scale;
+    t.k = k;
+    t.R = Q + (unit_i ? S : S * md.i_scale) * betta;
+    t.ks = unit_s ? k : k * md.s_scale;
     t.Rk = t.R * inv_k;
     return t;
+}
+
+// the table entry (k, beta, Q, 1/k) of coefficients alpha, beta, Q
+__host__ __device__ inline void medium_entry(int mode, double alpha, double betta, double Q, double* e)
+{
+    const double k = mode == RTS_MEDIUM_ABSORPTION ? alpha : alpha + betta;
+    e[0] = k;
+    e[1] = mode == RTS_MEDIUM_ABSORPTION ? 0.0 : betta;
+    e[2] = Q;
+    e[3] = k != 0.0 ? 1.0 / k : 0.0;  // k = 0: those nodes take the reference's expression
 }
 
 // The reference's own expressions, for the nodes outside the fast path
@@ -249,6 +255,12 @@ __device__ __noinline__ double node_illum_ref(int mode, double k, double ss, dou
     return (1 - ss * k) * (I0 + ss * R);
 }
 
+// The fast range 1e-3 <= x <= 700 as bounds on the high word of x (x >= 0,
+// and non-negative doubles order as their bit patterns): integer compares,
+// off the FP64 pipe.  The bounds are 1e-3 - 8e-10 and 700 + 1e-13.
+constexpr int kFastXLo = 0x3F50624D;  // high word of 1e-3
+constexpr int kFastXHi = 0x4085E000;  // high word of 700
+
 // GetCurIllum for one node at distance s from the in-face value I_0.  The
 // reference evaluates exp(-x) (I0 k + (exp(x) - 1) R) / k, x = k s (the
 // scattering form) or I0 exp(-x) + R (1 - exp(-x)) / k (the absorption
@@ -258,20 +270,22 @@ __device__ __noinline__ double node_illum_ref(int mode, double k, double ss, dou
 // one exponential and no division per node, the dominant FP64 cost.  Outside
 // that range the reference's own expression runs (including its overflow
 // past x = 709).
-__device__ inline double node_illum(const rts_medium& md, const CellTerms& t, double s, double I_0,
+__device__ inline double node_illum(const rts_medium& md, bool unit_i, const CellTerms& t, double s, double I_0,
                                     const double* __restrict__ tab)
 {
     const double x = t.ks * s;
-    const double I0 = md.i_scale == 1.0 ? I_0 : I_0 * md.i_scale;
+    const double I0 = unit_i ? I_0 : I_0 * md.i_scale;
+    const int hx = __double2hiint(x);
     double I;
-    if (x >= 1e-3 && x <= 700.0) {
+    if (hx >= kFastXLo && hx <= kFastXHi) {
+        // e I0 + (1 - e) R/k, as R/k + e (I0 - R/k): a subtraction and an FMA
         const double e = exp_neg(-x, tab);
-        I = e * I0 + (1 - e) * t.Rk;
+        I = fma(e, I0 - t.Rk, t.Rk);
     } else {
         I = node_illum_ref(md.mode, t.k, md.s_scale == 1.0 ? s : s * md.s_scale, I0, t.R);
     }
-    if (I < 0) return 0.0;
-    return md.i_scale == 1.0 ? I : I / md.i_scale;
+    if (__double2hiint(I) < 0) I = 0.0;  // I < 0 (the sign bit, tested as an integer)
+    return unit_i ? I : I / md.i_scale;
 }
 
 // ReCalcIllum's term |old - cur| / cur for one face (Illum_async.cpp:488-493),
@@ -313,6 +327,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
     const double* Sd = a.S + d * N;
     double* Il = a.illum + d * N * 4;
     const bool ball = a.md.radius > 0;
+    const bool unit_i = a.md.i_scale == 1.0, unit_s = a.md.s_scale == 1.0;
     __shared__ double tab[32];
     if (threadIdx.x < 32) tab[threadIdx.x] = a.exp2tab[threadIdx.x];
     __syncthreads();
@@ -340,7 +355,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
             const double2 m01 = *reinterpret_cast<const double2*>(a.med + 4 * c);
             const double2 m23 = *reinterpret_cast<const double2*>(a.med + 4 * c + 2);
             const double Sc = Sd[c];
-            const CellTerms cell = cell_terms(a.md, m01.x, m01.y, m23.x, m23.y, Sc);
+            const CellTerms cell = cell_terms(a.md, unit_i, unit_s, m01.x, m01.y, m23.x, m23.y, Sc);
             const double* sr = recs + 3 * (int64_t)i;
             double I[3];
 #pragma unroll
@@ -354,9 +369,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
                     const double* x = a.nodes + 36 * c + 9 * f + 3 * m;
                     const double d0 = x[0] - a.md.ball[0], d1 = x[1] - a.md.ball[1], d2 = x[2] - a.md.ball[2];
                     if (sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius)
-                        t = cell_terms(a.md, a.md.ball_alpha, a.md.ball_beta, a.md.ball_q, a.ball_inv_k, Sc);
+                        t = cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc);
                 }
-                I[m] = node_illum(a.md, t, sr[m], I_x0, tab);
+                I[m] = node_illum(a.md, unit_i, t, sr[m], I_x0, tab);
             }
             const double mean = (I[0] + I[1] + I[2]) * (1.0 / 3.0);
             norm_term(pick(f, f01.x, f01.y, f23.x, f23.y), mean, loc);
@@ -384,14 +399,6 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
 }
 
 // ---------------------------------------------------------------- host side
-
-// 1 / k of GetCurIllum's coefficients (0 where k is 0: those nodes take the
-// reference's expression)
-double medium_inv_k(const rts_medium& md, double alpha, double betta)
-{
-    const double k = md.mode == RTS_MEDIUM_ABSORPTION ? alpha : alpha + betta;
-    return k != 0.0 ? 1.0 / k : 0.0;
-}
 
 void exp2_table(double* tab)
 {
@@ -898,12 +905,7 @@ extern "C" int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const do
     rts_sweep_state& sw = *ctx->sweep;
     const int64_t N = sw.N;
     std::vector<double> m((size_t)(4 * N));
-    for (int64_t c = 0; c < N; ++c) {
-        m[4 * c] = alpha[c];
-        m[4 * c + 1] = beta[c];
-        m[4 * c + 2] = Q[c];
-        m[4 * c + 3] = medium_inv_k(*md, alpha[c], beta[c]);
-    }
+    for (int64_t c = 0; c < N; ++c) medium_entry(md->mode, alpha[c], beta[c], Q[c], &m[4 * c]);
     RTS_CUDA_TRY(ctx, cudaMemcpy(sw.d_med, m.data(), rts_bytes<double>(4 * N), cudaMemcpyHostToDevice));
     sw.md = *md;
     if (bc)
@@ -934,7 +936,7 @@ static int enqueue_sweep(rts_ctx* ctx, cudaStream_t st)
     a.md = sw.md;
     for (int i = 0; i < 4; ++i) a.bc[i] = sw.bc[i];
     exp2_table(a.exp2tab);
-    a.ball_inv_k = medium_inv_k(sw.md, sw.md.ball_alpha, sw.md.ball_beta);
+    medium_entry(sw.md.mode, sw.md.ball_alpha, sw.md.ball_beta, sw.md.ball_q, a.ball);
     a.norm = sw.d_norm;
     if (sw.D > 0) {
         rts_timing_begin(ctx, st);
