@@ -521,6 +521,16 @@ int rts_sweep_export_direction(rts_ctx* ctx, int64_t d, int32_t* order, int32_t*
 int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const double* alpha, const double* beta,
                          const double* Q, const double* bc);
 
+/* Class 11 of GetCurIllum (Illum_async.cpp:419-447), the medium coupled to
+ * the gas: for each cell, from its density and pressure in code units
+ * (flux_t::d, flux_t::p), alpha = beta = d DENSITY sigma_thomson / m_hydrogen
+ * and Q = alpha Ie(T), T = min(1e-6 p PRESSURE / (d DENSITY R_gas), 5000),
+ * with the reference's units and constants (global_value.h:32-52); *md is set
+ * to the scattering form with s_scale = DIST and i_scale = RADIATION.  Host
+ * only.  Pass the result to rts_sweep_set_medium. */
+int rts_sweep_medium_gas(int64_t N, const double* density, const double* pressure, double* alpha, double* beta,
+                         double* Q, rts_medium* md);
+
 /* One sweep of every local direction (the direction loops of
  * MPI_CalculateIllumAsync, solve_module/illum/Illum_async.cpp:726-784 and
  * 827-885) on `stream`: reads the device scattering array [local][N] and

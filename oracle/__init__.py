@@ -100,6 +100,7 @@ _SIG = {
     "orc_sweep_x0": (_i64, [_i64, _dp, _dp, _dp, C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),
     "orc_sweep_dir": (C.c_double, [_i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _dp, C.c_void_p, _dp,
                                    C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "orc_medium_gas": (None, [_i64, _dp, _dp, _dp, _dp, _dp, C.c_void_p]),
     "orc_sweep_all": (C.c_double, [_i64, _i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _i64p, _dp,
                                    C.c_void_p, _dp, C.c_void_p, _dp, _dp, _dp, _dp, _dp, C.c_int]),
 }
@@ -311,6 +312,17 @@ def medium(mode=0, s_scale=1.0, i_scale=1.0, ball=(0.0, 0.0, 0.0), radius=0.0, b
     m.radius = radius
     m.ball_alpha, m.ball_beta, m.ball_q = ball_coef
     return m
+
+
+def medium_gas(density, pressure):
+    """Class 11 of GetCurIllum: (Medium, alpha, beta, Q) from the gas state."""
+    d = np.ascontiguousarray(density, dtype=np.float64)
+    p = np.ascontiguousarray(pressure, dtype=np.float64)
+    n = d.size
+    a, b, q = np.empty(n), np.empty(n), np.empty(n)
+    md = Medium()
+    lib().orc_medium_gas(n, _p(d), _p(p), _p(a), _p(b), _p(q), C.byref(md))
+    return md, a, b, q
 
 
 def cube_mesh(n: int, bound_rule: int = 1, tilt: bool = True):

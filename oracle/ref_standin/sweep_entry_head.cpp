@@ -9,7 +9,7 @@
 extern "C" double ref_sweep_dirs(int count_cells, int ndir, const int* pairs_in, const int* order_in,
                                  const int* states_in, const long long* rec_off, const double* rec_s,
                                  const unsigned char* rec_face, const double* nodes, const double* scattering,
-                                 int class_vtk, double* illum)
+                                 int class_vtk, const double* density, const double* pressure, double* illum)
 {
     solve_mode.class_vtk = class_vtk;
     const int size_1_section = ndir;
@@ -36,6 +36,8 @@ extern "C" double ref_sweep_dirs(int count_cells, int ndir, const int* pairs_in,
                 vec_x[c].x[f][n] = Vector3(nodes[36 * c + 9 * f + 3 * n], nodes[36 * c + 9 * f + 3 * n + 1],
                                            nodes[36 * c + 9 * f + 3 * n + 2]);
     phys_local.assign(count_cells, flux_t{});
+    if (density && pressure)
+        for (int c = 0; c < count_cells; ++c) phys_local[c].d = density[c], phys_local[c].p = pressure[c];
     grid_t grid;
     grid.size = count_cells;
     grid.Illum = illum;

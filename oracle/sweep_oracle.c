@@ -469,6 +469,40 @@ static double sw_cur_illum(const orc_medium* md, double alpha, double betta, dou
     return I / md->i_scale;
 }
 
+/* Class 11 of GetCurIllum (Illum_async.cpp:419-447) as a medium: per cell
+ * alpha = beta = d (sigma_thomson / m_hydrogen), Q = alpha Ie(T) from the gas
+ * density and pressure in code units, with the reference's units and
+ * constants (global_value.h:32-52, the macros expanded as written there);
+ * the medium gets s_scale = DIST, i_scale = RADIATION. */
+void orc_medium_gas(int64_t N, const double* density, const double* pressure, double* alpha, double* beta, double* Q,
+                    orc_medium* md)
+{
+    const double PI_ = 3.14159265358979323846, C_LIGHT_ = 299792458.0;
+    const double DENSITY_ = (3.34 * 10e-14), VELOCITY_ = (3 * 1e8);
+    const double PRESSURE_ = (DENSITY_ * VELOCITY_ * VELOCITY_);
+    const double RADIATION_ = (DENSITY_ * VELOCITY_ * VELOCITY_ * VELOCITY_);
+    const double R_gas = 8.314, h_plank = 6.62 * 1e-34, k_boltzmann = 1.38 * 1e-23;
+    const double sigma_thomson = 6.652 * 1e-29, m_hydrogen = 1.6735575 * 1e-27;
+    for (int64_t c = 0; c < N; ++c) {
+        const double d = density[c] * DENSITY_;
+        const double p = pressure[c] * PRESSURE_;
+        double T = 1e-6 * p / (d * R_gas);
+        if (T > 5000.) T = 5000.;
+        const double T1 = k_boltzmann * PI_ * T;
+        const double T2 = T1 * T1;
+        const double T4 = T2 * T2;
+        const double Ie = T4 * 2 / (15 * h_plank * h_plank * h_plank * C_LIGHT_ * C_LIGHT_);
+        const double betta = d * (sigma_thomson / m_hydrogen);
+        alpha[c] = betta;
+        beta[c] = betta;
+        Q[c] = betta * Ie;
+    }
+    memset(md, 0, sizeof(*md));
+    md->mode = 0;
+    md->s_scale = 1e6;
+    md->i_scale = RADIATION_;
+}
+
 /* One direction: cells in `order`, x0 records (s, face) in the same order,
  * S [N] the scattering of this direction, bc [4] the intensities of boundary
  * codes -1..-4, coef [N*4*3] scratch; writes illum [N][4] (face means) and

@@ -33,6 +33,7 @@ from ._native import (  # noqa: F401
     header_symbols,
     load_library,
     medium,
+    medium_gas,
     mesh_cube,
 )
 from .build import build_library  # noqa: F401

@@ -127,6 +127,7 @@ _SIGNATURES = {
     "rts_sweep_import_direction": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _i64]),
     "rts_sweep_export_direction": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _i64, C.POINTER(_i64)]),
     "rts_sweep_set_medium": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _dp]),
+    "rts_sweep_medium_gas": (C.c_int, [_i64, _dp, _dp, _dp, _dp, _dp, _vp]),
     "rts_sweep": (C.c_int, [_vp, C.c_int, _dp]),
     "rts_sweep_exp_check": (C.c_int, [_vp, _i64, _dp]),
     "rts_illum_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.POINTER(_i64), _dp]),
@@ -152,6 +153,19 @@ def medium(mode=MEDIUM_SCATTERING, s_scale=1.0, i_scale=1.0, ball=(0.0, 0.0, 0.0
     m.radius = radius
     m.ball_alpha, m.ball_beta, m.ball_q = ball_coef
     return m
+
+
+def medium_gas(density, pressure):
+    """Class 11 of GetCurIllum: (Medium, alpha, beta, Q) from the gas density
+    and pressure per cell (code units); host only."""
+    d = np.ascontiguousarray(density, dtype=np.float64)
+    p = np.ascontiguousarray(pressure, dtype=np.float64)
+    n = d.size
+    a, b, q = np.empty(n), np.empty(n), np.empty(n)
+    md = Medium()
+    _status(load_library().rts_sweep_medium_gas(n, _ptr(d), _ptr(p), _ptr(a), _ptr(b), _ptr(q), C.byref(md)),
+            "rts_sweep_medium_gas")
+    return md, a, b, q
 
 
 # byte layout of the reference's cell_local records (LocX0<k>.bin)

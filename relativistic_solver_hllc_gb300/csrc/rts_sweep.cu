@@ -1046,3 +1046,46 @@ extern "C" int rts_sweep_exp_check(rts_ctx* ctx, int64_t n, double* max_ulp)
     ctx->launches++;
     return RTS_OK;
 }
+
+// The reference's unit system and constants (global_value.h:32-52): code units
+// of length, density, pressure and radiation, and SI physical constants.
+namespace gas {
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kCLight = 299792458.0;
+constexpr double kDist = 1e6;
+constexpr double kVelocity = 3 * 1e8;
+constexpr double kDensity = 3.34 * 10e-14;
+constexpr double kPressure = kDensity * kVelocity * kVelocity;
+constexpr double kRadiation = kDensity * kVelocity * kVelocity * kVelocity;
+constexpr double kRGas = 8.314;
+constexpr double kHPlank = 6.62 * 1e-34;
+constexpr double kBoltzmann = 1.38 * 1e-23;
+constexpr double kSigmaThomson = 6.652 * 1e-29;
+constexpr double kMHydrogen = 1.6735575 * 1e-27;
+}  // namespace gas
+
+extern "C" int rts_sweep_medium_gas(int64_t N, const double* density, const double* pressure, double* alpha,
+                                    double* beta, double* Q, rts_medium* md)
+{
+    if (N < 0 || (N > 0 && (!density || !pressure || !alpha || !beta || !Q)) || !md) return RTS_ERR_INVALID_ARGUMENT;
+    using namespace gas;
+    for (int64_t c = 0; c < N; ++c) {
+        const double d = density[c] * kDensity;
+        const double p = pressure[c] * kPressure;
+        const double T = std::min(1e-6 * p / (d * kRGas), 5000.);
+        const double T1 = kBoltzmann * kPi * T;
+        const double T2 = T1 * T1;
+        const double T4 = T2 * T2;
+        const double Ie = T4 * 2 / (15 * kHPlank * kHPlank * kHPlank * kCLight * kCLight);
+        const double betta = d * (kSigmaThomson / kMHydrogen);
+        alpha[c] = betta;
+        beta[c] = betta;
+        Q[c] = betta * Ie;
+    }
+    *md = rts_medium{};
+    md->mode = RTS_MEDIUM_SCATTERING;
+    md->s_scale = kDist;
+    md->i_scale = kRadiation;
+    return RTS_OK;
+}
+

@@ -25,8 +25,8 @@ sys.path.insert(0, str(HERE.parent.parent))
 import oracle  # noqa: E402
 
 VP = C.c_void_p
-# reference classes of GetCurIllum pinned here (class 11 needs the gas state)
-CLASSES = (0, 1, 2, 3, 10)
+# reference classes of GetCurIllum pinned here (class 11 reads the gas state)
+CLASSES = (0, 1, 2, 3, 10, 11)
 
 
 def ref_lib():
@@ -87,14 +87,18 @@ def main():
     rng = np.random.default_rng(seed)
     S = rng.uniform(0.0, 2.0, (M, N))
     il0 = rng.uniform(0.1, 1.0, (M, N, 4))
+    gas = np.random.default_rng(seed + 1)
+    density = gas.uniform(0.5, 2.0, N)
+    pressure = 10.0 ** gas.uniform(-8.0, -5.0, N)  # T below and at the 5000 K cap
     out, norms = {}, {}
     for cls in CLASSES:
         il = il0.copy()
         norms[cls] = L.ref_sweep_dirs(N, M, p(pairs), p(order), p(states), p(off), p(s), p(face), p(nodes), p(S),
-                                      cls, p(il))
+                                      cls, p(density), p(pressure), p(il))
         out[cls] = il
     np.savez_compressed(HERE / "sweep_classes_n2_m16.npz", n=n, M=M, bound_rule=1, tilt=1, seed=seed,
-                        S_pin=S.ravel()[:8], il0_pin=il0.ravel()[:8], classes=np.array(CLASSES),
+                        S_pin=S.ravel()[:8], il0_pin=il0.ravel()[:8], density=density, pressure=pressure,
+                        classes=np.array(CLASSES),
                         **{f"illum_{c}": out[c] for c in CLASSES}, norms=np.array([norms[c] for c in CLASSES]))
     print("wrote sweep_structs_n3_m12.npz, sweep_classes_n2_m16.npz")
 

@@ -2,7 +2,7 @@
 
 tests/golden/make_sweep_golden.py ran the reference's build_graph ordering,
 make_illum_struct nodes and characteristic records, and the sweep loop of
-MPI_CalculateIllumAsync (with GetCurIllum for classes 0, 1, 2, 3, 10,
+MPI_CalculateIllumAsync (with GetCurIllum for classes 0, 1, 2, 3, 10, 11,
 BoundaryConditions and ReCalcIllum), compiled from the reference source text,
 on small tilted cube meshes.  The oracle must reproduce those outputs bit for
 bit (same operation order, no fused multiply-adds); the device sweep, run on
@@ -53,25 +53,41 @@ def sweep_inputs(g, N, M):
     return S, il0
 
 
-@pytest.mark.parametrize("cls", [0, 1, 2, 3, 10])
+def oracle_medium(g, cls, N):
+    if cls == 11:
+        return oracle.medium_gas(g["density"], g["pressure"])
+    (a, b, q), kw = CLASS_MEDIUM[cls]
+    return oracle.medium(**kw), np.full(N, a), np.full(N, b), np.full(N, q)
+
+
+@pytest.mark.parametrize("cls", [0, 1, 2, 3, 10, 11])
 def test_oracle_sweep_equals_the_reference(cls):
     g = np.load(GOLDEN / "sweep_classes_n2_m16.npz")
     vert, pairs, normals, xyz, _, _ = case_inputs(g)
     st = oracle.SweepStructures(vert, pairs, normals, xyz)
     N, M = st.N, st.D
     S, il = sweep_inputs(g, N, M)
-    (a, b, q), kw = CLASS_MEDIUM[cls]
-    norm = oracle.sweep(st, S, np.full(N, a), np.full(N, b), np.full(N, q), il, md=oracle.medium(**kw),
-                        use_nodes=True)
+    md, a, b, q = oracle_medium(g, cls, N)
+    norm = oracle.sweep(st, S, a, b, q, il, md=md, use_nodes=True)
     assert np.array_equal(il, g[f"illum_{cls}"])
     ref_norm = g["norms"][list(g["classes"]).index(cls)]
     assert norm == ref_norm or (np.isnan(norm) and np.isnan(ref_norm))
 
 
+def test_gas_medium_equals_the_oracle(native_lib):
+    from relativistic_solver_hllc_gb300 import medium_gas
+
+    g = np.load(GOLDEN / "sweep_classes_n2_m16.npz")
+    md, a, b, q = medium_gas(g["density"], g["pressure"])
+    md2, a2, b2, q2 = oracle.medium_gas(g["density"], g["pressure"])
+    assert np.array_equal(a, a2) and np.array_equal(b, b2) and np.array_equal(q, q2)
+    assert (md.mode, md.s_scale, md.i_scale) == (md2.mode, md2.s_scale, md2.i_scale)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("cls", [0, 1, 2, 3, 10])
+@pytest.mark.parametrize("cls", [0, 1, 2, 3, 10, 11])
 def test_device_sweep_on_reference_structures(ctx, cls):
-    from relativistic_solver_hllc_gb300 import LOCX0_DTYPE, medium
+    from relativistic_solver_hllc_gb300 import LOCX0_DTYPE, medium, medium_gas
 
     g = np.load(GOLDEN / "sweep_classes_n2_m16.npz")
     vert, pairs, normals, xyz, area, fa = case_inputs(g)
@@ -87,8 +103,12 @@ def test_device_sweep_on_reference_structures(ctx, cls):
         rec["in_face_id"] = st.face[a0:a1]
         ctx.sweep_import_direction(d, st.order[d], st.states[d], rec)
     S, il0 = sweep_inputs(g, N, M)
-    (a, b, q), kw = CLASS_MEDIUM[cls]
-    ctx.sweep_set_medium(medium(**kw), np.full(N, a), np.full(N, b), np.full(N, q))
+    if cls == 11:
+        md, a, b, q = medium_gas(g["density"], g["pressure"])
+    else:
+        (a, b, q), kw = CLASS_MEDIUM[cls]
+        md, a, b, q = medium(**kw), np.full(N, a), np.full(N, b), np.full(N, q)
+    ctx.sweep_set_medium(md, a, b, q)
     ctx.send_scattering(S)
     ctx.copy_illum(il0.ravel())
     ctx.sweep()
