@@ -51,25 +51,24 @@ __host__ __device__ inline void face_verts(int f, int& a, int& b, int& c)
 
 // ---------------------------------------------------------------- geometry
 
-// IntersectionWithPlane (utils/grid_geometry/geometry_solve.cpp:109-128): the
-// point where x + t dir meets the plane through A, B, C.
-__device__ inline void plane_hit(const double* A, const double* B, const double* C, const double* x, const double* dir,
-                                 double* res)
-{
-    const double a = A[1] * (B[2] - C[2]) + B[1] * (C[2] - A[2]) + C[1] * (A[2] - B[2]);
-    const double b = A[0] * (C[2] - B[2]) + B[0] * (A[2] - C[2]) + C[0] * (B[2] - A[2]);
-    const double c = A[0] * (B[1] - C[1]) + B[0] * (C[1] - A[1]) + C[0] * (A[1] - B[1]);
-    const double d = A[0] * (C[1] * B[2] - B[1] * C[2]) + B[0] * (A[1] * C[2] - C[1] * A[2]) +
-                     C[0] * (B[1] * A[2] - A[1] * B[2]);
-    const double t = -(a * x[0] + b * x[1] + c * x[2] + d) / (a * dir[0] + b * dir[1] + c * dir[2]);
-    for (int i = 0; i < 3; ++i) res[i] = dir[i] * t + x[i];
-}
+// Everything about an in-face that the characteristic test needs and that
+// does not depend on the direction or the node, computed once per face:
+//   [0..3]   the plane a x + b y + c z + d = 0 through A, B, C with the
+//            coefficients IntersectionWithPlane forms
+//            (utils/grid_geometry/geometry_solve.cpp:109-128);
+//   [4..9]   the plane frame v1, v2 of SetBasis (:8-43) for the cell's
+//            outward face normal n;
+//   [10..13] B and C in that frame (Make2dPoint, :45-56, relative to A; A
+//            itself maps to (0, 0)).
+constexpr int kFrame = 16;  // doubles per face (14 used)
 
-// InTriangle (geometry_solve.cpp:129-159) in the plane frame of SetBasis /
-// Make2dPoint (:8-56): X strictly inside triangle ABC of the plane with
-// normal n.
-__device__ inline bool in_triangle(const double* A, const double* B, const double* C, const double* n, const double* X)
+__device__ inline void face_frame(const double* A, const double* B, const double* C, const double* n, double* F)
 {
+    F[0] = A[1] * (B[2] - C[2]) + B[1] * (C[2] - A[2]) + C[1] * (A[2] - B[2]);
+    F[1] = A[0] * (C[2] - B[2]) + B[0] * (A[2] - C[2]) + C[0] * (B[2] - A[2]);
+    F[2] = A[0] * (B[1] - C[1]) + B[0] * (C[1] - A[1]) + C[0] * (A[1] - B[1]);
+    F[3] = A[0] * (C[1] * B[2] - B[1] * C[2]) + B[0] * (A[1] * C[2] - C[1] * A[2]) +
+           C[0] * (B[1] * A[2] - A[1] * B[2]);
     double v1[3], v2[3];
     if (fabs(n[1]) < 1e-20) {
         v1[0] = 0, v1[1] = 1, v1[2] = 0;
@@ -85,26 +84,55 @@ __device__ inline bool in_triangle(const double* A, const double* B, const doubl
     const double z1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
     const double z2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
     for (int i = 0; i < 3; ++i) v1[i] /= z1, v2[i] /= z2;
-    double q[4][2];
-    const double* P[4] = {A, B, C, X};
-#pragma unroll
-    for (int p = 0; p < 4; ++p) {
+    const double* P[2] = {B, C};
+    for (int p = 0; p < 2; ++p) {
         double u = 0, w = 0;
         for (int k = 0; k < 3; ++k) {
             u += (P[p][k] - A[k]) * v1[k];
             w += (P[p][k] - A[k]) * v2[k];
         }
-        q[p][0] = u, q[p][1] = w;
+        F[10 + 2 * p] = u, F[11 + 2 * p] = w;
     }
-    const double r1 = (q[0][0] - q[3][0]) * (q[1][1] - q[0][1]) - (q[1][0] - q[0][0]) * (q[0][1] - q[3][1]);
-    const double r2 = (q[1][0] - q[3][0]) * (q[2][1] - q[1][1]) - (q[2][0] - q[1][0]) * (q[1][1] - q[3][1]);
-    const double r3 = (q[2][0] - q[3][0]) * (q[0][1] - q[2][1]) - (q[0][0] - q[2][0]) * (q[2][1] - q[3][1]);
+    for (int i = 0; i < 3; ++i) F[4 + i] = v1[i], F[7 + i] = v2[i];
+}
+
+__global__ void __launch_bounds__(256) sweep_frames_kernel(const double* __restrict__ vert,
+                                                           const double* __restrict__ normals, int64_t N,
+                                                           double* __restrict__ frames)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 4 * N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = i >> 2;
+        const int g = (int)(i & 3);
+        int ia, ib, ic;
+        face_verts(g, ia, ib, ic);
+        const double* v = vert + 12 * c;
+        face_frame(v + 3 * ia, v + 3 * ib, v + 3 * ic, normals + 3 * i, frames + kFrame * i);
+    }
+}
+
+// The characteristic from node x back along dir meets the plane of in-face F
+// at X (IntersectionWithPlane); InTriangle (geometry_solve.cpp:129-159):
+// X strictly inside the triangle, in the face's 2-D frame.
+__device__ inline bool hits_face(const double* __restrict__ F, const double* A, const double* x, const double* dir,
+                                 double* X)
+{
+    const double t = -(F[0] * x[0] + F[1] * x[1] + F[2] * x[2] + F[3]) / (F[0] * dir[0] + F[1] * dir[1] + F[2] * dir[2]);
+    for (int i = 0; i < 3; ++i) X[i] = dir[i] * t + x[i];
+    double u = 0, w = 0;
+    for (int k = 0; k < 3; ++k) {
+        u += (X[k] - A[k]) * F[4 + k];
+        w += (X[k] - A[k]) * F[7 + k];
+    }
+    const double bu = F[10], bw = F[11], cu = F[12], cw = F[13];
+    const double r1 = (0.0 - u) * (bw - 0.0) - (bu - 0.0) * (0.0 - w);
+    const double r2 = (bu - u) * (cw - bw) - (cu - bu) * (bw - w);
+    const double r3 = (cu - u) * (0.0 - cw) - (0.0 - cu) * (cw - w);
     return (r1 < 0 && r2 < 0 && r3 < 0) || (r1 > 0 && r2 > 0 && r3 > 0);
 }
 
 struct X0Args {
     const double* vert;      // [N][4][3]
-    const double* normals;   // [N][4][3]
+    const double* frames;    // [N][4][kFrame]
     const double* nodes;     // [N][4][3][3]
     const double* dirs;      // [D][3]
     const uint8_t* states;   // [D][N] in-face flags
@@ -143,8 +171,7 @@ __global__ void __launch_bounds__(256) sweep_x0_kernel(X0Args a)
                 int ia, ib, ic;
                 face_verts(g, ia, ib, ic);
                 double x0[3];
-                plane_hit(v + 3 * ia, v + 3 * ib, v + 3 * ic, x, dir, x0);
-                if (in_triangle(v + 3 * ia, v + 3 * ib, v + 3 * ic, a.normals + 12 * c + 3 * g, x0)) {
+                if (hits_face(a.frames + kFrame * (4 * c + g), v + 3 * ia, x, dir, x0)) {
                     const double d0 = x[0] - x0[0], d1 = x[1] - x0[1], d2 = x[2] - x0[2];
                     sv = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                     found = g;
@@ -716,10 +743,20 @@ extern "C" int rts_sweep_build(rts_ctx* ctx, int64_t* records, int64_t* levels)
         rts_dfree(ctx, sblk, rts_bytes<uint8_t>(std::max<int64_t>(D * N, 16)));
         return rc;
     }
-    // device: in-face and distance of every node
+    // device: the in-face frames, then the in-face and distance of every node
+    void* fblk = nullptr;
+    if ((rc = rts_dmalloc(ctx, &fblk, rts_bytes<double>(kFrame * 4 * N), "sweep face frames")) != RTS_OK) {
+        rts_dfree(ctx, sblk, rts_bytes<uint8_t>(std::max<int64_t>(D * N, 16)));
+        return rc;
+    }
+    if (N > 0) {
+        sweep_frames_kernel<<<(unsigned)std::min<int64_t>((4 * N + 255) / 256, 8192), 256, 0, st>>>(
+            sw.d_vert, sw.d_normals, N, (double*)fblk);
+        ctx->launches++;
+    }
     X0Args a;
     a.vert = sw.d_vert;
-    a.normals = sw.d_normals;
+    a.frames = (const double*)fblk;
     a.nodes = sw.d_nodes;
     a.dirs = ctx->d_xyz + 3 * ctx->out_start;
     a.states = (const uint8_t*)sblk;
@@ -735,11 +772,13 @@ extern "C" int rts_sweep_build(rts_ctx* ctx, int64_t* records, int64_t* levels)
         const cudaError_t e = cudaGetLastError();
         cudaStreamSynchronize(st);
         rts_dfree(ctx, sblk, rts_bytes<uint8_t>(std::max<int64_t>(D * N, 16)));
+        rts_dfree(ctx, fblk, rts_bytes<double>(kFrame * 4 * N));
         if (e != cudaSuccess)
             return rts_fail(ctx, RTS_ERR_CUDA, "launch of sweep_x0_kernel failed: %s", cudaGetErrorString(e));
         ctx->launches++;
     } else {
         rts_dfree(ctx, sblk, rts_bytes<uint8_t>(16));
+        rts_dfree(ctx, fblk, rts_bytes<double>(kFrame * 4 * N));
     }
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     if ((rc = check_flag(ctx, "rts_sweep_build")) != RTS_OK) return rc;
