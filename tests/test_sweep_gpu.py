@@ -213,3 +213,39 @@ def test_sweep_exponential_within_two_ulp_of_cuda(ctx):
     """The sweep's table-driven exp against CUDA's exp over [-700, 0]: each is
     within about an ulp of the exact value, so they differ by at most 2."""
     assert ctx.sweep_exp_check(1 << 22) <= 2.0
+
+
+def warp(x, eps):
+    """A smooth deformation of the cube (a function of position, so the
+    cells sharing a vertex move it together): irregular tetrahedra."""
+    s = np.sin(2 * np.pi * x)
+    return x + eps * np.stack([s[..., 1] * s[..., 2], s[..., 2] * s[..., 0], s[..., 0] * s[..., 1]], -1)
+
+
+def test_sweep_on_a_warped_mesh(ctx):
+    vert, pairs, _ = mesh_cube(4, 1, True)
+    vert = warp(vert, 0.05)
+    normals = oracle.face_normals(vert)
+    M = 48
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    N = vert.shape[0]
+    ctx.init(xyz, area, fa, N)
+    ctx.sweep_set_mesh(vert, pairs, normals)
+    ctx.sweep_build()
+    st = oracle.SweepStructures(vert, pairs, normals, xyz)
+    for d in (0, 17, 47):
+        order, states, recs = ctx.sweep_export_direction(d)
+        assert np.array_equal(order, st.order[d]) and np.array_equal(states, st.states[d])
+        a0, a1 = st.rec_off[d], st.rec_off[d + 1]
+        assert np.array_equal(recs["in_face_id"], st.face[a0:a1].astype(np.uint8))
+    a, b, q = coefficients(N, 8, "random")
+    ctx.sweep_set_medium(medium(), a, b, q, (0.2, 0.0, 1.0, 0.0))
+    il0 = np.random.default_rng(12).uniform(0.1, 1.0, (M, N, 4))
+    S = ctx.scattering(il0.ravel()).reshape(M, N)
+    ref = il0.copy()
+    n_ref = oracle.sweep(st, S, a, b, q, ref, bc=(0.2, 0.0, 1.0, 0.0))
+    n_dev = ctx.sweep()
+    got = np.empty(M * N * 4)
+    ctx.read_illum(got)
+    assert rel_err(got, ref.ravel()) <= TOL
+    assert same_norm(n_dev, n_ref)
