@@ -249,3 +249,38 @@ def test_sweep_on_a_warped_mesh(ctx):
     ctx.read_illum(got)
     assert rel_err(got, ref.ravel()) <= TOL
     assert same_norm(n_dev, n_ref)
+
+
+def test_direction_shards_equal_the_whole(native_lib):
+    """The reference shards the sweep by direction over its ranks
+    (Illum_async.cpp:726-784 on each rank's local directions).  Two contexts
+    owning directions [0, 10) and [10, 24) -- each sweeping its own rows of
+    Illum with the scattering of its own out-directions -- reproduce the
+    single-context sweep bit for bit, and the larger of their norms is its
+    norm.  (The contexts run one after the other on the one GPU.)"""
+    from relativistic_solver_hllc_gb300 import Context
+
+    M = 24
+    vert, pairs, normals = mesh_cube(3, 1, True)
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    N = vert.shape[0]
+    a, b, q = coefficients(N, 6, "random")
+    il0 = np.random.default_rng(21).uniform(0.1, 1.0, M * N * 4)
+
+    def run(start, end):
+        with Context(0) as c:
+            c.init(xyz, area, fa, N, start, end)
+            c.sweep_set_mesh(vert, pairs, normals)
+            c.sweep_build()
+            c.sweep_set_medium(medium(), a, b, q)
+            c.scattering(il0)  # S of the local out-directions from il0; leaves il0 on the device
+            norm = c.sweep()
+            out = np.empty(M * N * 4)
+            c.read_illum(out)
+        return out.reshape(M, N * 4)[start:end], norm
+
+    whole, n_whole = run(0, M)
+    lo, n_lo = run(0, 10)
+    hi, n_hi = run(10, M)
+    assert np.array_equal(np.concatenate([lo, hi]), whole)
+    assert max(n_lo, n_hi) == n_whole
