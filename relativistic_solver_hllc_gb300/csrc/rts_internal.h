@@ -42,7 +42,7 @@ constexpr int64_t RTS_RESID_CAP = 4096;
 
 // Split-precision operands of one source iteration (tensor-core path).
 struct rts_batch;
-constexpr int RTS_HOST_CHUNKS = 8;  // cell ranges of a pipelined host-buffer call
+constexpr int RTS_HOST_CHUNKS = 16;  // cell ranges of a pipelined host-buffer call
 
 struct rts_tune_entry {  // autotuned tile width of the tensor-core kernel
     int64_t M = 0;
