@@ -284,3 +284,28 @@ def test_direction_shards_equal_the_whole(native_lib):
     hi, n_hi = run(10, M)
     assert np.array_equal(np.concatenate([lo, hi]), whole)
     assert max(n_lo, n_hi) == n_whole
+
+
+def test_import_rejects_inconsistent_files(ctx):
+    """rts_sweep_import_direction checks the reference's files against the
+    mesh: the record count the face states imply, an order that lists
+    upstream cells first, and records naming in-faces only."""
+    M = 4
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 2, M)
+    ctx.sweep_build()
+    order, states, recs = ctx.sweep_export_direction(1)
+    with pytest.raises(RtsError) as e:
+        ctx.sweep_import_direction(1, order, states, recs[:-3])
+    assert e.value.status == _native.ERR_INVALID_ARGUMENT
+    with pytest.raises(RtsError) as e:
+        ctx.sweep_import_direction(1, order[::-1].copy(), states, recs)
+    assert e.value.status == _native.ERR_INVALID_ARGUMENT
+    bad = recs.copy()
+    c0 = int(order[0])
+    out_face = next(f for f in range(4) if not (int(states[c0]) >> f) & 1)
+    bad["in_face_id"][0] = out_face
+    with pytest.raises(RtsError) as e:
+        ctx.sweep_import_direction(1, order, states, bad)
+    assert e.value.status == _native.ERR_INVALID_ARGUMENT
+    # the consistent files are accepted and sweep as built
+    ctx.sweep_import_direction(1, order, states, recs)
