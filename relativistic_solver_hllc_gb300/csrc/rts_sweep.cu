@@ -141,6 +141,7 @@ struct X0Args {
     int32_t* const* steps;   // [D]
     const int32_t* nsteps;   // [D]
     int64_t N;
+    int64_t d0;              // first direction of this launch (grid y covers at most 65535)
     int* flag;               // set when a node finds no in-face
 };
 
@@ -150,7 +151,7 @@ struct X0Args {
 // Grid: x over the items of a direction, y over the directions.
 __global__ void __launch_bounds__(256) sweep_x0_kernel(X0Args a)
 {
-    const int64_t d = blockIdx.y;
+    const int64_t d = a.d0 + blockIdx.y;
     const int64_t n = a.steps[d][a.nsteps[d]];
     uint32_t* items = a.items[d];
     double* recs = a.recs[d];
@@ -768,14 +769,18 @@ extern "C" int rts_sweep_build(rts_ctx* ctx, int64_t* records, int64_t* levels)
     a.flag = ctx->d_flag + 2;
     if (D > 0) {
         const int64_t per = std::max<int64_t>(1, std::min<int64_t>((2 * N + 255) / 256, 64));
-        sweep_x0_kernel<<<dim3((unsigned)per, (unsigned)D), 256, 0, st>>>(a);
-        const cudaError_t e = cudaGetLastError();
+        cudaError_t e = cudaSuccess;
+        for (int64_t d0 = 0; d0 < D && e == cudaSuccess; d0 += 65535) {
+            a.d0 = d0;
+            sweep_x0_kernel<<<dim3((unsigned)per, (unsigned)std::min<int64_t>(D - d0, 65535)), 256, 0, st>>>(a);
+            e = cudaGetLastError();
+            ctx->launches++;
+        }
         cudaStreamSynchronize(st);
         rts_dfree(ctx, sblk, rts_bytes<uint8_t>(std::max<int64_t>(D * N, 16)));
         rts_dfree(ctx, fblk, rts_bytes<double>(kFrame * 4 * N));
         if (e != cudaSuccess)
             return rts_fail(ctx, RTS_ERR_CUDA, "launch of sweep_x0_kernel failed: %s", cudaGetErrorString(e));
-        ctx->launches++;
     } else {
         rts_dfree(ctx, sblk, rts_bytes<uint8_t>(16));
         rts_dfree(ctx, fblk, rts_bytes<double>(kFrame * 4 * N));
