@@ -54,8 +54,13 @@ constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
 constexpr int G_CTAS_PER_SM = 1;
 constexpr uint32_t G_TMEM_COLS = 512;
 constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
-constexpr int G_BAR_BYTES = 512;  // ring, accumulator and relaxation barriers, TMEM address
-constexpr int G_REL_BUF = 2 * 1024;  // per epilogue warp: 2 buffers x (32 rows x 16 B hi, then 32 rows x 16 B lo)
+// relaxation row buffers per epilogue warp: G_REL_NB - 1 units are fetched
+// ahead of the one being relaxed
+constexpr int G_REL_NB = 2;
+// ring, accumulator and relaxation barriers (the relaxation's from index 16),
+// then the TMEM address
+constexpr int G_BAR_BYTES = (8 * (17 + G_REL_NB * G_EPI_WARPS) + 127) / 128 * 128;
+constexpr int G_REL_BUF = G_REL_NB * 1024;  // per epilogue warp: buffers of 32 rows x 16 B hi, then 32 rows x 16 B lo
 constexpr size_t G_REL_OFF = (size_t)G_STAGES * G_STAGE_BYTES + G_BAR_BYTES;
 constexpr size_t G_SMEM = G_REL_OFF + (size_t)G_EPI_WARPS * G_REL_BUF + 1024;
 static_assert(G_SMEM <= 227 * 1024, "shared memory per CTA");
@@ -150,7 +155,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G_STAGES * G_STAGE_BYTES);  // G_BAR_BYTES
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 48);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 16 + G_REL_NB * G_EPI_WARPS);
     const uint32_t smem_base = smem_u32(smem);
     const uint32_t bar_base = smem_u32(bars);
     auto full_bar = [&](int s) { return bar_base + 8u * s; };
@@ -158,7 +163,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     auto acc_full_bar = [&](int a) { return bar_base + 8u * (2 * G_STAGES + a); };
     auto acc_empty_bar = [&](int a) { return bar_base + 8u * (2 * G_STAGES + 2 + a); };
     // relaxation row buffers: barrier of buffer b of epilogue warp w
-    auto rel_bar = [&](int w, uint32_t b) { return bar_base + 8u * (16 + 2 * w + (int)b); };
+    auto rel_bar = [&](int w, uint32_t b) { return bar_base + 8u * (16 + G_REL_NB * w + (int)b); };
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -170,10 +175,8 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             mbar_init(acc_full_bar(a), 1);
             mbar_init(acc_empty_bar(a), G_EPI_WARPS);
         }
-        for (int w = 0; w < G_EPI_WARPS; ++w) {
-            mbar_init(rel_bar(w, 0), 1);
-            mbar_init(rel_bar(w, 1), 1);
-        }
+        for (int w = 0; w < G_EPI_WARPS; ++w)
+            for (int b = 0; b < G_REL_NB; ++b) mbar_init(rel_bar(w, (uint32_t)b), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -425,10 +428,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     return tf32 ? (k0 >> 4) * 64 + (k0 & 15) * 2 : (k0 >> 5) * 64 + (k0 & 31);
                 };
                 int u_next = 0;  // next unit to fetch
-                auto pump = [&](int u_cons) {  // keep one unit fetched beyond the one being consumed
-                    while (u_next < u_real && u_next <= u_cons + 1) {
+                auto pump = [&](int u_cons) {  // keep G_REL_NB - 1 units fetched beyond the one being consumed
+                    while (u_next < u_real && u_next <= u_cons + (G_REL_NB - 1)) {
                         if (lane == 0) {
-                            const uint32_t b = rel_issued & 1u, dst = rbuf_s + b * 1024u;
+                            const uint32_t b = rel_issued % G_REL_NB, dst = rbuf_s + b * 1024u;
                             const int x = unit_x(u_next);
                             bulk_wait_read0();  // the store that last read this buffer
                             mbar_expect_tx(rel_bar(ew, b), 1024);
@@ -506,8 +509,9 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     for (int ui = 0; ui < 8 / ucols; ++ui) {
                         const int u = e0 / ucols + ui;
                         if (u >= u_real) break;
-                        const uint32_t b = rel_used & 1u;
-                        const bool got = mbar_wait(rel_bar(ew, b), (rel_used >> 1) & 1u, flag, FLAG_WAIT_EPILOGUE);
+                        const uint32_t b = rel_used % G_REL_NB;
+                        const bool got =
+                            mbar_wait(rel_bar(ew, b), (rel_used / G_REL_NB) & 1u, flag, FLAG_WAIT_EPILOGUE);
                         ++rel_used;
                         if (!__all_sync(0xffffffffu, got)) {
                             stop = true;
