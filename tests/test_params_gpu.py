@@ -131,3 +131,36 @@ def test_write_solution_files(ctx, tmp_path):
                            ("divstream.bin", ds, 1), ("divimpuls.bin", di, 3)):
         n, got = read_counted(tmp_path / name, per)
         assert n == N and np.array_equal(got, ref.reshape(got.shape)), name
+
+
+def test_divergence_of_a_linear_stream(ctx):
+    """The analytic check of the reference's TestDivStream
+    (solve_module/illum/Illum_async.cpp:1351-1387): a stream (3x, 0, 0) at the
+    face centres has divergence 3 on every cell.  Through Illum: I_jf =
+    9 x_f (w_j)_x gives the face streams 9 x_f Q with Q = sum_j w_j (w_j)_x
+    area_j / full_area (1/3 for an exact quadrature), so divstream = 9 Q_x on
+    every cell of a real mesh (the divergence theorem on a linear field, with
+    face centres)."""
+    from relativistic_solver_hllc_gb300 import mesh_cube
+
+    vert, pairs, normals = mesh_cube(3, 1, True)
+    N, M = vert.shape[0], 146
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    FV = [[0, 1, 3], [1, 2, 3], [2, 0, 3], [0, 2, 1]]
+    centres = np.stack([vert[:, FV[f]].mean(axis=1) for f in range(4)], axis=1)  # [N][4][3]
+    fS = np.stack([0.5 * np.linalg.norm(np.cross(vert[:, FV[f][1]] - vert[:, FV[f][0]],
+                                                  vert[:, FV[f][2]] - vert[:, FV[f][0]]), axis=1)
+                   for f in range(4)], axis=1)
+    vol = np.abs(np.linalg.det(np.stack([vert[:, 1] - vert[:, 0], vert[:, 2] - vert[:, 0],
+                                         vert[:, 3] - vert[:, 0]], axis=1))) / 6
+    w = xyz.reshape(M, 3)
+    il = 9.0 * centres[None, :, :, 0] * w[:, 0][:, None, None]  # [M][N][4]
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(np.ascontiguousarray(il).ravel())
+    ctx.set_geometry(normals, fS, vol)
+    _, _, _, ds, _ = ctx.illum_params()
+    qx = float((w[:, 0] * w[:, 0] * area).sum() / fa)
+    assert abs(qx - 1 / 3) < 1e-3
+    # 1e-12 relative to the face terms 9 x_f Q_x S_f / V, which cancel to 9 Q_x
+    scale = 4 * 9 * qx * np.max(np.abs(centres[:, :, 0]) * fS, axis=1) / vol
+    assert float(np.max(np.abs(ds - 9 * qx) / scale)) <= 1e-12
