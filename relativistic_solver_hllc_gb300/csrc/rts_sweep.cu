@@ -40,6 +40,7 @@ namespace {
 // partial wave cost 11 %).
 constexpr int SWEEP_THREADS = 128;
 constexpr double SWEEP_EPS = 1e-10;  // `eps`, global_value.h:13
+constexpr int kExpTable = 256;       // entries 2^(j/256) of the sweep's exponential (exp_neg)
 
 __host__ __device__ inline void face_verts(int f, int& a, int& b, int& c)
 {
@@ -206,23 +207,27 @@ struct SweepArgs {
     int64_t N;
     rts_medium md;
     double bc[4];
-    double exp2tab[32];      // 2^(j/32)
+    double exp2tab[kExpTable];  // 2^(j/256)
     double ball[4];          // medium table entry of the ball's coefficients
     unsigned long long* norm;
 };
 
 // exp(x) for -700 <= x <= 0 by Tang's table-driven method (P. T. P. Tang,
 // "Table-driven implementation of the exponential function in IEEE
-// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (32 m + j) ln2/32 + r
-// with |r| <= ln2/64, exp(x) = 2^m 2^(j/32) (1 + p(r)), p the degree-6 Taylor
-// polynomial of exp(r) - 1 (truncation below 4e-18), 2^(j/32) from a 32-entry
-// table and 2^m added to the exponent field.  11 FP64 operations against the
-// general exp's range checks and longer polynomial; within 1 ulp of the exact
-// value over the range (checked against CUDA's exp by rts_sweep_exp_check).
-constexpr double kExpInvL = 46.16624130844683;            // 32 / ln 2
-constexpr double kExpLHi = 0.02166084939249829;           // ln 2 / 32, leading part
-constexpr double kExpLLo = 7.247021293269686e-19;         // ln 2 / 32 - kExpLHi
+// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (256 m + j) ln2/256
+// + r with |r| <= ln2/512, exp(x) = 2^m 2^(j/256) (1 + p(r)), 2^(j/256) from
+// a 256-entry table and 2^m added to the exponent field.  p(r) = r + r^2 h(r)
+// with h the quadratic fitted to (exp(r) - 1 - r) / r^2 on that interval by
+// weighted least squares at Chebyshev nodes (relative error of 1 + p below
+// 5.1e-18, against 1.1e-16 for one ulp).  9 FP64 operations against the
+// general exp's range checks and longer polynomial; within 1.03 ulp of the
+// exact value over the range (checked against CUDA's exp by
+// rts_sweep_exp_check).
+constexpr double kExpInvL = 369.3299304675746;            // 256 / ln 2
+constexpr double kExpLHi = 0.0027076061740622863;         // ln 2 / 256, leading part
+constexpr double kExpLLo = 9.058776616587108e-20;         // ln 2 / 256 - kExpLHi
 constexpr double kExpShift = 6755399441055744.0;          // 1.5 * 2^52: rounds to an integer
+constexpr double kExpH0 = 0.49999999999999795, kExpH1 = 0.16666668003070842, kExpH2 = 0.04166667023041113;
 
 __device__ __forceinline__ double exp_neg(double x, const double* __restrict__ tab)
 {
@@ -231,14 +236,11 @@ __device__ __forceinline__ double exp_neg(double x, const double* __restrict__ t
     const double N = t - kExpShift;
     double r = fma(-N, kExpLHi, x);
     r = fma(-N, kExpLLo, r);
-    double h = fma(r, 1.0 / 720, 1.0 / 120);
-    h = fma(r, h, 1.0 / 24);
-    h = fma(r, h, 1.0 / 6);
-    h = fma(r, h, 0.5);
+    const double h = fma(r, fma(r, kExpH2, kExpH1), kExpH0);
     const double p = fma(r * r, h, r);
-    const double T = tab[n & 31];
+    const double T = tab[n & (kExpTable - 1)];
     const double y = fma(T, p, T);
-    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> 5) << 52));
+    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> 8) << 52));
 }
 
 // Per-cell terms of GetCurIllum (solve_module/illum/Illum_async.cpp:259-470):
@@ -356,8 +358,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
     double* Il = a.illum + d * N * 4;
     const bool ball = a.md.radius > 0;
     const bool unit_i = a.md.i_scale == 1.0, unit_s = a.md.s_scale == 1.0;
-    __shared__ double tab[32];
-    if (threadIdx.x < 32) tab[threadIdx.x] = a.exp2tab[threadIdx.x];
+    __shared__ double tab[kExpTable];
+    for (int i = threadIdx.x; i < kExpTable; i += SWEEP_THREADS) tab[i] = a.exp2tab[i];
     __syncthreads();
     double loc = -1.0;
     {
@@ -430,15 +432,15 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
 
 void exp2_table(double* tab)
 {
-    for (int j = 0; j < 32; ++j) tab[j] = exp2((double)j / 32.0);
+    for (int j = 0; j < kExpTable; ++j) tab[j] = exp2((double)j / kExpTable);
 }
 
 // exp_neg against CUDA's exp at n points spread over [-700, 0] (and the 1e-3
 // end): the largest difference in units in the last place of CUDA's value.
 __global__ void exp_check_kernel(int64_t n, const double* __restrict__ tab_in, double* out)
 {
-    __shared__ double tab[32];
-    if (threadIdx.x < 32) tab[threadIdx.x] = tab_in[threadIdx.x];
+    __shared__ double tab[kExpTable];
+    for (int i = threadIdx.x; i < kExpTable; i += blockDim.x) tab[i] = tab_in[i];
     __syncthreads();
     double worst = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -1070,22 +1072,23 @@ extern "C" int rts_sweep_exp_check(rts_ctx* ctx, int64_t n, double* max_ulp)
 {
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     RTS_REQUIRE(ctx, n >= 2 && max_ulp, RTS_ERR_INVALID_ARGUMENT, "rts_sweep_exp_check: n >= 2 and an output");
-    double tab[32];
+    double tab[kExpTable];
     exp2_table(tab);
     void* p = nullptr;
-    int rc = rts_dmalloc(ctx, &p, 33 * sizeof(double), "exp check");
+    int rc = rts_dmalloc(ctx, &p, (kExpTable + 1) * sizeof(double), "exp check");
     if (rc != RTS_OK) return rc;
     double* d = (double*)p;
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
-    cudaError_t e = cudaMemcpyAsync(d, tab, 32 * sizeof(double), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d + 32, 0, sizeof(double), st);
+    cudaError_t e = cudaMemcpyAsync(d, tab, kExpTable * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + kExpTable, 0, sizeof(double), st);
     if (e == cudaSuccess) {
-        exp_check_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(n, d, d + 32);
+        exp_check_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, st>>>(n, d, d + kExpTable);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(max_ulp, d + 32, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(max_ulp, d + kExpTable, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    rts_dfree(ctx, d, 33 * sizeof(double));
+    rts_dfree(ctx, d, (kExpTable + 1) * sizeof(double));
     if (e != cudaSuccess) return rts_fail(ctx, RTS_ERR_CUDA, "rts_sweep_exp_check: %s", cudaGetErrorString(e));
     ctx->launches++;
     return RTS_OK;
