@@ -225,8 +225,11 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
     return RTS_OK;
 }
 
-// The same cell ranges as the host-buffer call, on the device Illum and into
-// the device S, all on `st` (no copies, no host synchronisation).
+// On the device Illum and into the device S, all on `st` (no copies, no host
+// synchronisation): one cell range over all cells -- with nothing to copy,
+// the host-buffer call's ranges would only multiply the launches.  The
+// range's problem is the host-buffer call's first (rebuilt when the call
+// alternates with host-buffer calls).
 int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
 {
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
@@ -234,9 +237,8 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     const int mode = rts_split_mode(precision);
     const int64_t N = ctx->N, M = ctx->M;
     const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
-    const int64_t tiles = (N + 127) / 128;
-    const int nch = (int)std::min<int64_t>(RTS_HOST_CHUNKS, tiles);
-    const int64_t csz = (tiles + nch - 1) / nch * 128;
+    const int nch = 1;
+    const int64_t csz = N;
     int rc;
     for (int i = 0; i < nch; ++i) {
         const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
