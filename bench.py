@@ -167,8 +167,9 @@ def sweep_medium(N: int, seed: int = 11):
 
 
 def read_sweep_profile():
-    """FP64 operations per cell-direction of sweep_kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "sweep_fp64.json"
+    """FP64 operations and DRAM bytes per cell-direction of sweep_kernel's read
+    form (the timed steps) from the committed ncu summary."""
+    p = ROOT / "profiles" / "sweep_kernel_24576x1000.json"
     try:
         return json.loads(p.read_text())
     except Exception:
@@ -222,6 +223,27 @@ def run_sweep(args, rank, world, local):
     kern_avg = kern_ms / max(kern_n, 1)
     value = N * M / (kern_avg / 1e3) / 1e9
 
+    # the other two forms of the kernel, timed alone: the sweep that stores
+    # the attenuation factors (the first after a change of medium) and sweeps
+    # that evaluate them every time (the cache switched off)
+    def timed_sweeps(n_sweeps):
+        ctx.kernel_timing(True)
+        for _ in range(n_sweeps):
+            ctx.sweep(read_norm=False)
+        ctx.sweep()
+        ms, cnt = ctx.kernel_timing(False)
+        return ms / max(cnt, 1)
+
+    ctx.sweep_set_medium(pkg.medium(), a, b, q)
+    store_ms = timed_sweeps(0)
+    ctx.set_tuning(_native.TUNE_SWEEP_CACHE, 0)
+    eval_ms = timed_sweeps(2)
+    ctx.set_tuning(_native.TUNE_SWEEP_CACHE, 1)
+    forms = {"read_ms": kern_avg, "store_ms": store_ms, "evaluate_ms": eval_ms,
+             "note": "read: the timed steps (attenuation factors exp(-k s) stored by the first sweep of the medium, "
+                     "read since); store: the first sweep after a change of medium; evaluate: "
+                     "RTS_TUNE_SWEEP_CACHE 0 (the exponential in every sweep, as the reference)"}
+
     # parity spot check on two full-size directions against the oracle
     accuracy = None
     if rank == 0 and args.check != "none":
@@ -254,12 +276,14 @@ def run_sweep(args, rank, world, local):
     ctx.illum_solve("fp16x3", max_iter=1 + 1, accuracy=0.0)  # warm-up of the split operands
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    ctx.sweep_set_medium(pkg.medium(), a, b, q)  # a new medium: the first sweep stores the factors again
     norms = ctx.illum_solve("fp16x3", max_iter=Ke, accuracy=0.0)
     e2e_s = time.perf_counter() - t0
     e2e = {"value": N * M * len(norms) / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": 0,
            "d2h_bytes_per_step": 8, "steps": len(norms),
-           "call": "rts_illum_solve (sweep + FP16x3 scattering per iteration, device-resident Illum and S, "
-                   "the 8-byte norm read back each iteration)"}
+           "call": "rts_sweep_set_medium, then rts_illum_solve (sweep + FP16x3 scattering per iteration, "
+                   "device-resident Illum and S, the 8-byte norm read back each iteration; the first sweep "
+                   "stores the attenuation factors, the others read them)"}
 
     prof = read_sweep_profile()
     fl = prof.get("fp64_flops_per_cell_dir")
@@ -269,8 +293,12 @@ def run_sweep(args, rank, world, local):
             "traffic": prof.get("dram_bytes_per_cell_dir") and prof["dram_bytes_per_cell_dir"] * N * M,
             "peak_source": "nominal GB300 FP64 (no measured FP64 peak available)",
             "fp64_pipe_active": prof.get("fp64_pipe_active_frac"),
-            "note": "achieved = FP64 operations per cell-direction counted by ncu (dadd + dmul + 2 dfma) x the "
-                    "measured cell-direction rate",
+            "note": "achieved = FP64 operations per cell-direction of the read form counted by ncu "
+                    "(dadd + dmul + 2 dfma) x the measured cell-direction rate; the pipe also issues the compares, "
+                    "so fp64_pipe_active (ncu, 24,576 x 1000) is the binding figure",
+            "hbm": {"algorithmic_bytes_per_cell_dir": prof.get("algorithmic_bytes_per_cell_dir"),
+                    "achieved_gbs": prof.get("algorithmic_bytes_per_cell_dir") and
+                    prof["algorithmic_bytes_per_cell_dir"] * value, "peak_gbs": peak_value(load_peaks()[0], "hbm_gbs") or FALLBACK_PEAKS["hbm_gbs"]},
             "kernel_ms_avg": kern_avg, "kernel_launches_timed": kern_n}
 
     cpu = None
@@ -302,9 +330,11 @@ def run_sweep(args, rank, world, local):
                                f"directions, alpha~U(0.5,2) beta~U(0,1) Q~U(0,1), boundary x=0 source",
                    "cells": N, "dirs": M, "node_records": records, "max_steps": steps_max,
                    "structures_build_s": t_build, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (no flush)", "step": "one sweep of every direction"},
+                   "l2": "inputs larger than L2 (no flush)",
+                   "step": "one sweep of every direction within a source iteration (medium unchanged since the "
+                           "first sweep, which stored the attenuation factors: sweep_forms.store_ms)"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-        "accuracy": accuracy, "norm": norm, "wall_ms_per_step": elapsed / (K + 1) * 1e3,
+        "accuracy": accuracy, "norm": norm, "wall_ms_per_step": elapsed / (K + 1) * 1e3, "sweep_forms": forms,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -577,6 +577,14 @@ int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, 
 #define RTS_TUNE_SERVE_POLICY 3
 #define RTS_TUNE_SERVE_BUDGET 4
 #define RTS_TUNE_SERVE_SLACK 5
+/*   RTS_TUNE_SWEEP_CACHE: 1 (default) the first rts_sweep after a change of
+ *   the medium or of the structures stores every node's attenuation factor
+ *   exp(-k s) (8 bytes per node record, allocated then; within budget), and
+ *   the sweeps after it read the factor instead of evaluating it -- the same
+ *   numbers, without the exponential; 0 every sweep evaluates them (and the
+ *   factors are not allocated).  A sweep that cannot allocate the factors
+ *   evaluates them. */
+#define RTS_TUNE_SWEEP_CACHE 6
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* Autotuner of the tensor-core kernel's tile width (out-directions per

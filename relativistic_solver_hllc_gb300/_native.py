@@ -64,6 +64,7 @@ TUNE_BIAS = 2   # RTS_TUNE_BIAS
 TUNE_SERVE_POLICY = 3  # RTS_TUNE_SERVE_POLICY
 TUNE_SERVE_BUDGET = 4  # RTS_TUNE_SERVE_BUDGET
 TUNE_SERVE_SLACK = 5  # RTS_TUNE_SERVE_SLACK
+TUNE_SWEEP_CACHE = 6  # RTS_TUNE_SWEEP_CACHE
 
 _dp = C.POINTER(C.c_double)
 _i64 = C.c_int64

@@ -840,6 +840,11 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
         RTS_REQUIRE(ctx, value >= 0, RTS_ERR_INVALID_ARGUMENT, "tile budget %d below 0", value);
         ctx->serve_budget = value;
         return RTS_OK;
+    case RTS_TUNE_SWEEP_CACHE:
+        RTS_REQUIRE(ctx, value == 0 || value == 1, RTS_ERR_INVALID_ARGUMENT, "sweep cache switch %d not 0 or 1", value);
+        ctx->sweep_cache = value;
+        if (ctx->sweep) ctx->sweep->att_valid = false;
+        return RTS_OK;
     case RTS_TUNE_BIAS:
         RTS_REQUIRE(ctx, value >= -1, RTS_ERR_INVALID_ARGUMENT, "bias correction %d below -1", value);
         ctx->split_bias = value;

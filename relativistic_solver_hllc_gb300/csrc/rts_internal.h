@@ -94,6 +94,11 @@ struct rts_sweep_state {
     std::vector<int64_t> h_nitems;
     std::vector<std::pair<void*, size_t>> blocks;  // allocations behind the tables
     std::vector<char> have;          // direction d built or imported
+    double** d_att = nullptr;        // device pointer table [D] of the attenuation factors
+    std::vector<double*> h_att;
+    double* att_blk = nullptr;       // one factor per node record (exp(-k s), or a negative mark)
+    size_t att_bytes = 0;
+    bool att_valid = false;          // stored by a sweep since the last change of medium or structures
     double* d_med = nullptr;         // [N][4] k, beta, Q, 1/k (k = alpha + beta, or alpha)
     rts_medium md{};
     double bc[4] = {0.0, 0.0, 1.0, 0.0};
@@ -155,6 +160,7 @@ struct rts_ctx {
     int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
     int tuning_epoch = 0;        // bumped when a setting that batch tables copy changes
     int64_t w_version = 0;       // bumped whenever d_W is rewritten
+    int sweep_cache = 1;         // rts_sweep: store the attenuation factors once per medium (RTS_TUNE_SWEEP_CACHE)
     int serve_policy = 1;        // rts_serve_run: 0 all resident, 1 earliest deadline first, 2 least remaining work first
     int64_t serve_budget = 0;    // tiles per step for policy 1 (0: 8 waves of the SMs)
     int serve_slack = 500;       // policy 1 deadline: arrival + serve_slack / 100 x estimated isolated time

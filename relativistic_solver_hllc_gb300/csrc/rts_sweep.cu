@@ -139,6 +139,7 @@ struct X0Args {
     const uint8_t* states;   // [D][N] in-face flags
     uint32_t* const* items;  // [D]
     double* const* recs;     // [D]
+    double* const* att;      // [D] attenuation factors, parallel to recs (stored or read by the cached forms)
     int32_t* const* steps;   // [D]
     const int32_t* nsteps;   // [D]
     int64_t N;
@@ -195,6 +196,7 @@ __global__ void __launch_bounds__(256) sweep_x0_kernel(X0Args a)
 struct SweepArgs {
     uint32_t* const* items;  // [D]
     double* const* recs;     // [D]
+    double* const* att;      // [D] attenuation factors, parallel to recs (stored or read by the cached forms)
     int32_t* const* steps;   // [D]
     uint32_t* const* bnd;    // [D]
     const int32_t* nsteps;   // [D]
@@ -300,18 +302,32 @@ constexpr int kFastXHi = 0x4085E000;  // high word of 700
 // one exponential and no division per node, the dominant FP64 cost.  Outside
 // that range the reference's own expression runs (including its overflow
 // past x = 709).
-__device__ inline double node_illum(const rts_medium& md, bool unit_i, const CellTerms& t, double s, double I_0,
-                                    const double* __restrict__ tab)
+//
+// The node's attenuation factor e depends on the medium and the node's
+// distance only, not on I_0 or the source S: node_att gives e, or kAttRef
+// (negative; e never is) where the reference's expression has to run, and
+// node_value the node from it.  Within a source iteration the medium stays,
+// so the factors can be stored by one sweep and read by the next ones.
+constexpr double kAttRef = -1.0;
+
+__device__ inline double node_att(const CellTerms& t, double s, const double* __restrict__ tab)
 {
     const double x = t.ks * s;
-    const double I0 = unit_i ? I_0 : I_0 * md.i_scale;
     const int hx = __double2hiint(x);
+    return (hx >= kFastXLo && hx <= kFastXHi) ? exp_neg(-x, tab) : kAttRef;
+}
+
+// s is read only on the reference's path (sr: the node's distance record)
+__device__ inline double node_value(const rts_medium& md, bool unit_i, const CellTerms& t, double e,
+                                    const double* sr, double I_0)
+{
+    const double I0 = unit_i ? I_0 : I_0 * md.i_scale;
     double I;
-    if (hx >= kFastXLo && hx <= kFastXHi) {
+    if (__double2hiint(e) >= 0) {
         // e I0 + (1 - e) R/k, as R/k + e (I0 - R/k): a subtraction and an FMA
-        const double e = exp_neg(-x, tab);
         I = fma(e, I0 - t.Rk, t.Rk);
     } else {
+        const double s = *sr;
         I = node_illum_ref(md.mode, t.k, md.s_scale == 1.0 ? s : s * md.s_scale, I0, t.R);
     }
     if (__double2hiint(I) < 0) I = 0.0;  // I < 0 (the sign bit, tested as an integer)
@@ -320,7 +336,10 @@ __device__ inline double node_illum(const rts_medium& md, bool unit_i, const Cel
 
 // ReCalcIllum's term |old - cur| / cur for one face (Illum_async.cpp:488-493),
 // folded into the running max.  The division runs only when the term can
-// raise the max; NaN terms (0 / 0) drop out as in the reference.
+// raise the max; NaN terms (0 / 0) drop out as in the reference.  (A screen
+// of the terms on the exponent fields with integer operations, to spare the
+// multiply and compare, measured 4-7 % slower: the kernel is issue-bound as
+// much as FP64-bound.)
 __device__ inline void norm_term(double old, double cur, double& loc)
 {
     const double d = fabs(old - cur);
@@ -346,6 +365,9 @@ __device__ inline int pick(int g, int v0, int v1, int v2, int v3)
 // (visible after the barrier); it writes its mean to the face and to the
 // neighbour's copy.  Every face is written once per sweep, so each writer
 // takes ReCalcIllum's term against the old value.
+// kAtt: 0 evaluates every node's attenuation factor, 1 also stores it,
+// 2 reads the stored factors (no exponential).
+template <int kAtt>
 __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
 {
     const int64_t d = blockIdx.x;
@@ -358,9 +380,12 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
     double* Il = a.illum + d * N * 4;
     const bool ball = a.md.radius > 0;
     const bool unit_i = a.md.i_scale == 1.0, unit_s = a.md.s_scale == 1.0;
-    __shared__ double tab[kExpTable];
-    for (int i = threadIdx.x; i < kExpTable; i += SWEEP_THREADS) tab[i] = a.exp2tab[i];
-    __syncthreads();
+    double* att = kAtt ? a.att[d] : nullptr;
+    __shared__ double tab[kAtt == 2 ? 1 : kExpTable];
+    if (kAtt != 2) {
+        for (int i = threadIdx.x; i < kExpTable; i += SWEEP_THREADS) tab[i] = a.exp2tab[i];
+        __syncthreads();
+    }
     double loc = -1.0;
     {
         const uint32_t* bnd = a.bnd[d];
@@ -401,7 +426,14 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
                     if (sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius)
                         t = cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc);
                 }
-                I[m] = node_illum(a.md, unit_i, t, sr[m], I_x0, tab);
+                double e;
+                if (kAtt == 2) {
+                    e = att[3 * (int64_t)i + m];
+                } else {
+                    e = node_att(t, sr[m], tab);
+                    if (kAtt == 1) att[3 * (int64_t)i + m] = e;
+                }
+                I[m] = node_value(a.md, unit_i, t, e, sr + m, I_x0);
             }
             const double mean = (I[0] + I[1] + I[2]) * (1.0 / 3.0);
             norm_term(pick(f, f01.x, f01.y, f23.x, f23.y), mean, loc);
@@ -528,6 +560,8 @@ int alloc_tables(rts_ctx* ctx, rts_sweep_state& sw)
     sw.d_items = (uint32_t**)p;
     if ((rc = rts_dmalloc(ctx, &p, sizeof(double*) * D, "sweep record table")) != RTS_OK) return rc;
     sw.d_recs = (double**)p;
+    if ((rc = rts_dmalloc(ctx, &p, sizeof(double*) * D, "sweep attenuation table")) != RTS_OK) return rc;
+    sw.d_att = (double**)p;
     if ((rc = rts_dmalloc(ctx, &p, sizeof(int32_t*) * D, "sweep step table")) != RTS_OK) return rc;
     sw.d_steps = (int32_t**)p;
     if ((rc = rts_dmalloc(ctx, &p, sizeof(uint32_t*) * D, "sweep boundary table")) != RTS_OK) return rc;
@@ -538,6 +572,7 @@ int alloc_tables(rts_ctx* ctx, rts_sweep_state& sw)
     sw.d_nbnd = (int32_t*)p;
     sw.h_items.assign(D, nullptr);
     sw.h_recs.assign(D, nullptr);
+    sw.h_att.assign(D, nullptr);
     sw.h_steps.assign(D, nullptr);
     sw.h_bnd.assign(D, nullptr);
     sw.h_nsteps.assign(D, 0);
@@ -551,6 +586,10 @@ void free_blocks(rts_ctx* ctx, rts_sweep_state& sw)
 {
     for (auto& b : sw.blocks) rts_dfree(ctx, b.first, b.second);
     sw.blocks.clear();
+    rts_dfree(ctx, sw.att_blk, sw.att_bytes);
+    sw.att_blk = nullptr;
+    sw.att_bytes = 0;
+    sw.att_valid = false;
     std::fill(sw.h_items.begin(), sw.h_items.end(), nullptr);
     std::fill(sw.h_recs.begin(), sw.h_recs.end(), nullptr);
     std::fill(sw.h_steps.begin(), sw.h_steps.end(), nullptr);
@@ -611,6 +650,7 @@ void rts_sweep_free(rts_ctx* ctx)
     rts_dfree(ctx, sw->d_norm, sizeof(unsigned long long));
     rts_dfree(ctx, sw->d_items, sizeof(uint32_t*) * D);
     rts_dfree(ctx, sw->d_recs, sizeof(double*) * D);
+    rts_dfree(ctx, sw->d_att, sizeof(double*) * D);
     rts_dfree(ctx, sw->d_steps, sizeof(int32_t*) * D);
     rts_dfree(ctx, sw->d_bnd, sizeof(uint32_t*) * D);
     rts_dfree(ctx, sw->d_nsteps, rts_bytes<int32_t>(D));
@@ -884,6 +924,7 @@ extern "C" int rts_sweep_import_direction(rts_ctx* ctx, int64_t d, const int32_t
     RTS_CUDA_TRY(ctx, cudaMemcpy(lblk, steps.data(), rts_bytes<int32_t>(steps.size()), cudaMemcpyHostToDevice));
     if (!bnd.empty())
         RTS_CUDA_TRY(ctx, cudaMemcpy(bblk, bnd.data(), rts_bytes<uint32_t>(bnd.size()), cudaMemcpyHostToDevice));
+    sw.att_valid = false;
     if (sw.have[d]) sw.records -= 3 * sw.h_nitems[d];
     sw.records += 3 * (int64_t)items.size();
     sw.h_items[d] = (uint32_t*)iblk;
@@ -959,16 +1000,58 @@ extern "C" int rts_sweep_set_medium(rts_ctx* ctx, const rts_medium* md, const do
     else
         sw.bc[0] = 0.0, sw.bc[1] = 0.0, sw.bc[2] = 1.0, sw.bc[3] = 0.0;
     sw.has_medium = true;
+    sw.att_valid = false;
+    return RTS_OK;
+}
+
+// The form of the next sweep: 2 reads the stored attenuation factors, 1
+// stores them (laying out, and where needed allocating, their block), 0
+// evaluates them (the cache switched off, or no room for the factors).
+static int att_mode(rts_ctx* ctx, rts_sweep_state& sw, cudaStream_t st, int* mode)
+{
+    *mode = 0;
+    if (!ctx->sweep_cache) return RTS_OK;
+    if (sw.att_valid) {
+        *mode = 2;
+        return RTS_OK;
+    }
+    int64_t nrec = 0;
+    for (int64_t d = 0; d < sw.D; ++d) nrec += 3 * sw.h_nitems[d];
+    const size_t need = rts_bytes<double>(std::max<int64_t>(nrec, 2));
+    if (sw.att_bytes != need) {
+        rts_dfree(ctx, sw.att_blk, sw.att_bytes);
+        sw.att_blk = nullptr;
+        sw.att_bytes = 0;
+        const std::string keep = ctx->last_error;
+        void* p = nullptr;
+        if (rts_dmalloc(ctx, &p, need, "sweep attenuation factors") != RTS_OK) {
+            ctx->last_error = keep;  // not an error: this sweep evaluates the factors
+            return RTS_OK;
+        }
+        sw.att_blk = (double*)p;
+        sw.att_bytes = need;
+    }
+    int64_t o = 0;
+    for (int64_t d = 0; d < sw.D; ++d) {
+        sw.h_att[d] = sw.att_blk + o;
+        o += 3 * sw.h_nitems[d];
+    }
+    RTS_CUDA_TRY(ctx, cudaMemcpyAsync(sw.d_att, sw.h_att.data(), sizeof(double*) * sw.D, cudaMemcpyHostToDevice, st));
+    *mode = 1;
     return RTS_OK;
 }
 
 static int enqueue_sweep(rts_ctx* ctx, cudaStream_t st)
 {
     rts_sweep_state& sw = *ctx->sweep;
+    int mode = 0;
+    int rc = att_mode(ctx, sw, st, &mode);
+    if (rc != RTS_OK) return rc;
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(sw.d_norm, 0, sizeof(unsigned long long), st));
     SweepArgs a;
     a.items = sw.d_items;
     a.recs = sw.d_recs;
+    a.att = sw.d_att;
     a.steps = sw.d_steps;
     a.bnd = sw.d_bnd;
     a.nsteps = sw.d_nsteps;
@@ -986,10 +1069,16 @@ static int enqueue_sweep(rts_ctx* ctx, cudaStream_t st)
     a.norm = sw.d_norm;
     if (sw.D > 0) {
         rts_timing_begin(ctx, st);
-        sweep_kernel<<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
+        if (mode == 2)
+            sweep_kernel<2><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
+        else if (mode == 1)
+            sweep_kernel<1><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
+        else
+            sweep_kernel<0><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
         rts_timing_end(ctx, st);
         RTS_CHECK_LAUNCH(ctx, "sweep_kernel");
         ctx->launches++;
+        if (mode == 1) sw.att_valid = true;
     }
     return RTS_OK;
 }

@@ -103,13 +103,17 @@ def test_sweep_matches_oracle(ctx, kind, mode):
     assert same_norm(n_dev, n_ref), (n_dev, n_ref)
 
 
-def oracle_solve(st, xyz, area, fa, il, S, a, b, q, md, bc, iters, accuracy):
+def oracle_solve(st, xyz, area, fa, il, S, a, b, q, md, bc, iters, accuracy, W=None):
+    """Sweeps and scattering integrals alternated as in the reference's
+    CalculateIllum loop; W (M x M) replaces the Thomson integral when given."""
     N, D = st.N, st.D
     norms = []
     for it in range(iters):
         norms.append(oracle.sweep(st, S, a, b, q, il, md=md, bc=bc))
-        if iters > 1:
+        if iters > 1 and W is None:
             S = oracle.calculate_int_cpu(N, xyz, area, fa, il.ravel()).reshape(D, N)
+        elif iters > 1:
+            S = oracle.scatter_matrix(W, oracle.face_mean(il.ravel(), N, D))
         if not norms[-1] > accuracy:
             break
     return np.array(norms), S
@@ -133,6 +137,74 @@ def test_illum_solve_matches_oracle(ctx, precision, tol):
     assert len(norms) == len(ref_norms) == 6
     assert rel_err(got, il.ravel()) <= tol, rel_err(got, il.ravel())
     assert rel_err(norms[1:], ref_norms[1:]) <= 1e-9 if precision == "fp64" else True
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL), ("fp16x3", 1e-6)])
+def test_illum_solve_hg_phase(ctx, precision, tol):
+    """The source iteration with the Henyey-Greenstein phase function (g = 0.6)
+    between sweeps: the device's weights against the oracle's HG matrix."""
+    M, g = 24, 0.6
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 3, M)
+    ctx.set_phase(_native.PHASE_HG, g)
+    ctx.sweep_build()
+    st = oracle.SweepStructures(vert, pairs, normals, xyz)
+    a, b, q = coefficients(N, 5, "random")
+    bc = (0.0, 0.0, 1.0, 0.0)
+    ctx.sweep_set_medium(medium(), a, b, q, bc)
+    il = np.zeros((M, N, 4))
+    ctx.copy_illum(il.ravel())
+    norms = ctx.illum_solve(precision, max_iter=5, accuracy=1e-300)
+    W = oracle.weights_hg(xyz, area, g)
+    ref_norms, _ = oracle_solve(st, xyz, area, fa, il, np.zeros((M, N)), a, b, q, oracle.medium(), bc, 5, 1e-300,
+                                W=W)
+    got = np.empty(M * N * 4)
+    ctx.read_illum(got)
+    assert len(norms) == len(ref_norms) == 5
+    assert rel_err(got, il.ravel()) <= tol, rel_err(got, il.ravel())
+
+
+def test_stored_attenuation_factors_give_the_same_sweep(ctx):
+    """The sweep that stores the nodes' attenuation factors, the sweeps that
+    read them and the sweeps that evaluate them (RTS_TUNE_SWEEP_CACHE 0) give
+    the same Illum and norm bit for bit; a new medium replaces the factors."""
+    M = 14
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 3, M)
+    ctx.sweep_build()
+    il0 = np.random.default_rng(21).uniform(0.1, 1.0, M * N * 4)
+    ctx.scattering(il0)  # the source term of the sweeps
+    media = [(medium(), *coefficients(N, 6, "random")),
+             (medium(), *coefficients(N, 7, "thin")),  # nodes on the reference's expression
+             (medium(ball=(0.5, 0.5, 0.5), radius=0.3, ball_coef=(3.0, 0.5, 0.2)), *coefficients(N, 8, "random")),
+             (medium(MEDIUM_ABSORPTION, s_scale=2.0, i_scale=0.5), *coefficients(N, 9, "random"))]
+    results = []
+    for md, a, b, q in media:
+        ctx.set_tuning(_native.TUNE_SWEEP_CACHE, 1)
+        ctx.sweep_set_medium(md, a, b, q)
+        runs = []
+        for cache in (1, 1, 1, 0):  # stores, reads, reads, evaluates
+            if cache == 0:
+                ctx.set_tuning(_native.TUNE_SWEEP_CACHE, 0)
+            ctx.copy_illum(il0)
+            n = ctx.sweep()
+            got = np.empty(M * N * 4)
+            ctx.read_illum(got)
+            runs.append((n, got))
+        for n, got in runs[1:]:
+            assert np.array_equal(got, runs[0][1]) and n == runs[0][0]
+        assert all(not np.array_equal(runs[0][1], r) for r in results)
+        results.append(runs[0][1])
+    # factors stored under one medium are not read under the next
+    ctx.set_tuning(_native.TUNE_SWEEP_CACHE, 1)
+    md, a, b, q = media[0]
+    ctx.sweep_set_medium(md, a, b, q)
+    ctx.copy_illum(il0)
+    ctx.sweep()
+    ctx.sweep_set_medium(*media[1])
+    ctx.copy_illum(il0)
+    ctx.sweep()
+    got = np.empty(M * N * 4)
+    ctx.read_illum(got)
+    assert np.array_equal(got, results[1])
 
 
 def test_illum_solve_stops_at_accuracy(ctx):
