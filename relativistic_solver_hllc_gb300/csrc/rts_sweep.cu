@@ -304,31 +304,33 @@ constexpr int kFastXHi = 0x4085E000;  // high word of 700
 // past x = 709).
 //
 // The node's attenuation factor e depends on the medium and the node's
-// distance only, not on I_0 or the source S: node_att gives e, or kAttRef
-// (negative; e never is) where the reference's expression has to run, and
-// node_value the node from it.  Within a source iteration the medium stays,
-// so the factors can be stored by one sweep and read by the next ones.
+// distance only, not on I_0 or the source S: node_att gives e / 3 (the face
+// mean takes a third of each node), or kAttRef (negative; e never is) where
+// the reference's expression has to run.  Within a source iteration the
+// medium stays, so the factors can be stored by one sweep and read by the
+// next ones.
 constexpr double kAttRef = -1.0;
 
 __device__ inline double node_att(const CellTerms& t, double s, const double* __restrict__ tab)
 {
     const double x = t.ks * s;
     const int hx = __double2hiint(x);
-    return (hx >= kFastXLo && hx <= kFastXHi) ? exp_neg(-x, tab) : kAttRef;
+    return (hx >= kFastXLo && hx <= kFastXHi) ? exp_neg(-x, tab) * (1.0 / 3.0) : kAttRef;
 }
 
-// s is read only on the reference's path (sr: the node's distance record)
-__device__ inline double node_value(const rts_medium& md, bool unit_i, const CellTerms& t, double e,
+// A third of the node value from its factor e3 = e / 3 (s is read only on
+// the reference's path; sr: the node's distance record), clamped at 0.
+__device__ inline double node_third(const rts_medium& md, bool unit_i, const CellTerms& t, double e3,
                                     const double* sr, double I_0)
 {
     const double I0 = unit_i ? I_0 : I_0 * md.i_scale;
     double I;
-    if (__double2hiint(e) >= 0) {
-        // e I0 + (1 - e) R/k, as R/k + e (I0 - R/k): a subtraction and an FMA
-        I = fma(e, I0 - t.Rk, t.Rk);
+    if (__double2hiint(e3) >= 0) {
+        // (e I0 + (1 - e) R/k) / 3, as R/3k + e/3 (I0 - R/k)
+        I = fma(e3, I0 - t.Rk, t.Rk * (1.0 / 3.0));
     } else {
         const double s = *sr;
-        I = node_illum_ref(md.mode, t.k, md.s_scale == 1.0 ? s : s * md.s_scale, I0, t.R);
+        I = node_illum_ref(md.mode, t.k, md.s_scale == 1.0 ? s : s * md.s_scale, I0, t.R) * (1.0 / 3.0);
     }
     if (__double2hiint(I) < 0) I = 0.0;  // I < 0 (the sign bit, tested as an integer)
     return unit_i ? I : I / md.i_scale;
@@ -337,9 +339,9 @@ __device__ inline double node_value(const rts_medium& md, bool unit_i, const Cel
 // ReCalcIllum's term |old - cur| / cur for one face (Illum_async.cpp:488-493),
 // folded into the running max.  The division runs only when the term can
 // raise the max; NaN terms (0 / 0) drop out as in the reference.  (A screen
-// of the terms on the exponent fields with integer operations, to spare the
-// multiply and compare, measured 4-7 % slower: the kernel is issue-bound as
-// much as FP64-bound.)
+// of the terms on the exponent fields with integer operations, meant to spare
+// the multiply and compare, measured 4-7 % slower: as compiled it added FP64
+// operations instead of removing them.)
 __device__ inline void norm_term(double old, double cur, double& loc)
 {
     const double d = fabs(old - cur);
@@ -366,8 +368,9 @@ __device__ inline int pick(int g, int v0, int v1, int v2, int v3)
 // neighbour's copy.  Every face is written once per sweep, so each writer
 // takes ReCalcIllum's term against the old value.
 // kAtt: 0 evaluates every node's attenuation factor, 1 also stores it,
-// 2 reads the stored factors (no exponential).
-template <int kAtt>
+// 2 reads the stored factors (no exponential).  kUnitI: i_scale == 1 (no
+// scaling of the source and the node values, and the one-step face mean).
+template <int kAtt, bool kUnitI>
 __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
 {
     const int64_t d = blockIdx.x;
@@ -379,7 +382,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
     const double* Sd = a.S + d * N;
     double* Il = a.illum + d * N * 4;
     const bool ball = a.md.radius > 0;
-    const bool unit_i = a.md.i_scale == 1.0, unit_s = a.md.s_scale == 1.0;
+    constexpr bool unit_i = kUnitI;
+    const bool unit_s = a.md.s_scale == 1.0;
     double* att = kAtt ? a.att[d] : nullptr;
     __shared__ double tab[kAtt == 2 ? 1 : kExpTable];
     if (kAtt != 2) {
@@ -412,30 +416,50 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
             const double Sc = Sd[c];
             const CellTerms cell = cell_terms(a.md, unit_i, unit_s, m01.x, m01.y, m23.x, m23.y, Sc);
             const double* sr = recs + 3 * (int64_t)i;
-            double I[3];
+            double I0[3], e3[3];
+            bool inb[3] = {false, false, false};
 #pragma unroll
             for (int m = 0; m < 3; ++m) {
                 const int g = (int)((w >> (2 * m)) & 3u);
                 const int nbg = pick(g, pr.x, pr.y, pr.z, pr.w);
                 // CalculateIllumeOnInnerFace (Illum_async.cpp:172-199)
-                const double I_x0 = nbg < 0 ? a.bc[-nbg - 1] : pick(g, f01.x, f01.y, f23.x, f23.y);
-                CellTerms t = cell;
+                I0[m] = nbg < 0 ? a.bc[-nbg - 1] : pick(g, f01.x, f01.y, f23.x, f23.y);
                 if (ball) {  // class 0: other coefficients inside the ball
                     const double* x = a.nodes + 36 * c + 9 * f + 3 * m;
                     const double d0 = x[0] - a.md.ball[0], d1 = x[1] - a.md.ball[1], d2 = x[2] - a.md.ball[2];
-                    if (sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius)
-                        t = cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc);
+                    inb[m] = sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius;
                 }
-                double e;
                 if (kAtt == 2) {
-                    e = att[3 * (int64_t)i + m];
+                    e3[m] = att[3 * (int64_t)i + m];
                 } else {
-                    e = node_att(t, sr[m], tab);
-                    if (kAtt == 1) att[3 * (int64_t)i + m] = e;
+                    const CellTerms t =
+                        inb[m] ? cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc)
+                               : cell;
+                    e3[m] = node_att(t, sr[m], tab);
+                    if (kAtt == 1) att[3 * (int64_t)i + m] = e3[m];
                 }
-                I[m] = node_value(a.md, unit_i, t, e, sr + m, I_x0);
             }
-            const double mean = (I[0] + I[1] + I[2]) * (1.0 / 3.0);
+            // The face mean (I_0 + I_1 + I_2) / 3.  Where no node can clamp
+            // (R/k >= 0, every I0 >= 0 and every factor on the fast form: each
+            // node value R/k + e (I0 - R/k) is then >= 0, all sign bits tested
+            // at once) it is R/k + sum_m e_m/3 (I0_m - R/k): 3 subtractions and
+            // 3 FMAs instead of 6 operations for the nodes and 3 for the mean.
+            double mean;
+            if (unit_i && !ball &&
+                (__double2hiint(e3[0]) | __double2hiint(e3[1]) | __double2hiint(e3[2]) | __double2hiint(I0[0]) |
+                 __double2hiint(I0[1]) | __double2hiint(I0[2]) | __double2hiint(cell.Rk)) >= 0) {
+                const double Rk = cell.Rk;
+                mean = fma(e3[0], I0[0] - Rk, fma(e3[1], I0[1] - Rk, fma(e3[2], I0[2] - Rk, Rk)));
+            } else {
+                mean = 0.0;
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const CellTerms t =
+                        inb[m] ? cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc)
+                               : cell;
+                    mean += node_third(a.md, unit_i, t, e3[m], sr + m, I0[m]);
+                }
+            }
             norm_term(pick(f, f01.x, f01.y, f23.x, f23.y), mean, loc);
             Il[4 * c + f] = mean;
             const int nb = pick(f, pr.x, pr.y, pr.z, pr.w);
@@ -1069,12 +1093,22 @@ static int enqueue_sweep(rts_ctx* ctx, cudaStream_t st)
     a.norm = sw.d_norm;
     if (sw.D > 0) {
         rts_timing_begin(ctx, st);
-        if (mode == 2)
-            sweep_kernel<2><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
-        else if (mode == 1)
-            sweep_kernel<1><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
-        else
-            sweep_kernel<0><<<(unsigned)sw.D, SWEEP_THREADS, 0, st>>>(a);
+        const dim3 grid((unsigned)sw.D);
+        if (sw.md.i_scale == 1.0) {
+            if (mode == 2)
+                sweep_kernel<2, true><<<grid, SWEEP_THREADS, 0, st>>>(a);
+            else if (mode == 1)
+                sweep_kernel<1, true><<<grid, SWEEP_THREADS, 0, st>>>(a);
+            else
+                sweep_kernel<0, true><<<grid, SWEEP_THREADS, 0, st>>>(a);
+        } else {
+            if (mode == 2)
+                sweep_kernel<2, false><<<grid, SWEEP_THREADS, 0, st>>>(a);
+            else if (mode == 1)
+                sweep_kernel<1, false><<<grid, SWEEP_THREADS, 0, st>>>(a);
+            else
+                sweep_kernel<0, false><<<grid, SWEEP_THREADS, 0, st>>>(a);
+        }
         rts_timing_end(ctx, st);
         RTS_CHECK_LAUNCH(ctx, "sweep_kernel");
         ctx->launches++;
