@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-serve", action="store_true", help="skip the short serving stream of the default line")
+    ap.add_argument("--serve-window", type=float, default=2.0, help="arrival window of that stream, seconds")
     ap.add_argument("--flush", type=int, default=2, choices=[0, 1, 2],
                     help="tensor-core K-slices per FP32 drain (library default 1; 2 halves the drains and "
                          "still meets the 1e-6 gate on this workload, checked in the same run)")
@@ -578,32 +580,74 @@ def run_ours(args, rank, world, local):
     # host-buffer calls of the e2e leg replace the resident iteration)
     S_timed = ctx.solve_read() if (prec != "fp64" and args.check == "full") else None
 
-    # end-to-end through the host-buffer entry point (measured before the
-    # accuracy check's host-side comparisons of 5.3 GB arrays, which slowed
-    # the host copies that follow them by a quarter)
+    # end to end through the call the reference's solver makes: per step, the
+    # per-direction CudaSendIllumAsync copies of the FP64 face-layout Illum
+    # from pinned host memory, then the pair of
+    # CalculateIntScatteringAsyncMPIStream calls of the source iteration
+    # (solve_module/illum/Illum_async.cpp:1019-1020: [0, M/3) on scattering
+    # stream 1, [0, M) on scattering stream 2) at the bench's precision, each
+    # with its D2H of S into the pinned host scattering array, and the wait
+    # for both streams.  Measured before the accuracy check's host-side
+    # comparisons of 5.3 GB arrays, which slowed the host copies that follow
+    # them by a quarter.
     Ke = args.e2e_steps if args.e2e_steps is not None else K
     illum_host = ctx.host_illum()
     ctx.synth_illum(WORKLOAD["seed"], WORKLOAD["mu"], WORKLOAD["sigma"])
     ctx.read_illum(illum_host)
     S_host = ctx.host_scattering()
-    B_pin = _native.PinnedBuffer(N * 8)  # every input of the call from pinned host memory
-    B_host = B_pin.array(np.float64, N)
-    B_host[:] = B
-    ctx.scattering_update(prec, illum_host, B_host, lam, S_host)  # warm-up
+    ctx.set_precision(prec)
+    size_1 = M // 3
+
+    def reference_sequence():
+        for j in range(M):
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, illum_host)
+        ctx.scattering_async(0, size_1, pkg.STREAM_SCATTERING_1, S_host)
+        ctx.scattering_async(0, M, pkg.STREAM_SCATTERING_2, S_host)
+        ctx.sync_stream(pkg.STREAM_SCATTERING_1)
+        ctx.sync_stream(pkg.STREAM_SCATTERING_2)
+        ctx._keep.clear()
+
+    reference_sequence()  # warm-up: builds the stream slots' operands
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(Ke):
-        ctx.scattering_update(prec, illum_host, B_host, lam, S_host)
+        reference_sequence()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, dist)
+    ctx.set_precision("fp64")
     e2e = {"value": N * M * Ke * world / e2e_s / 1e9, "unit": UNIT,
-           "h2d_bytes_per_step": M * N * 4 * 8 + N * 8, "d2h_bytes_per_step": M * N * 8,
-           "steps": Ke, "call": "rts_scattering_update (pinned host buffers)"}
+           "h2d_bytes_per_step": M * N * 4 * 8, "d2h_bytes_per_step": (size_1 + M) * N * 8,
+           "steps": Ke, "ms_per_step": e2e_s / Ke * 1e3,
+           "call": f"the reference's calling sequence at {prec}: {M} x rts_send_illum_async (CudaSendIllumAsync, "
+                   f"pinned host Illum), rts_scattering_async [0,{size_1}) on stream 1 and [0,{M}) on stream 2 "
+                   "(CalculateIntScatteringAsyncMPIStream x 2, D2H of S into the pinned host array), "
+                   "rts_sync_stream x 2; cell-directions counted once per step"}
 
-    # accuracy against the FP64 path on identical inputs
+    # the same integral through the pipelined host-buffer entry point
+    # (rts_scattering_update: H2D of the FP64 Illum and B, integral + update,
+    # D2H of the FP64 S, over 16 cell ranges in flight)
+    B_pin = _native.PinnedBuffer(N * 8)  # every input of the call from pinned host memory
+    B_host = B_pin.array(np.float64, N)
+    B_host[:] = B
+    ctx.scattering_update(prec, illum_host, B_host, lam, S_host)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        ctx.scattering_update(prec, illum_host, B_host, lam, S_host)
+    e2e2_s = max_over_ranks(time.perf_counter() - t0, dist)
+    h2d, d2h = M * N * 4 * 8 + N * 8, M * N * 8
+    e2e_host_call = {"value": N * M * Ke * world / e2e2_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                     "d2h_bytes_per_step": d2h, "steps": Ke, "ms_per_step": e2e2_s / Ke * 1e3,
+                     "link_gbs": (h2d + d2h) / (e2e2_s / Ke) / 1e9,
+                     "call": "rts_scattering_update (pinned host buffers, 16 cell ranges pipelined)"}
+
+    # accuracy against the FP64 path on identical inputs; the FP64 steps are
+    # timed too (CUDA events on the kernel and around the steps): the plain
+    # FP64 GPU kernel's rate on the same workload in the same run
     accuracy = None
+    fp64_gpu = None
     if prec != "fp64" and args.check != "none":
         S_t = S_timed
         n_chk = K if args.check == "full" else 1
@@ -612,8 +656,22 @@ def run_ours(args, rank, world, local):
             ctx.solve_step(True)
             S_t = ctx.solve_read()
         fresh("fp64")
+        ctx.wait()
+        ctx.kernel_timing(True)
+        ev0.record(stream)
         for _ in range(n_chk):
             ctx.solve_step_async(True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        k64_ms, k64_n = ctx.kernel_timing(False)
+        step64_s = ev0.elapsed_time(ev1) / 1e3 / n_chk
+        fp64_step = N * M / step64_s / 1e9
+        fp64_gpu = {"value": fp64_step, "unit": UNIT, "ms_per_step": step64_s * 1e3,
+                    "kernel_ms_avg": k64_ms / max(k64_n, 1), "kernel_launches_timed": k64_n,
+                    "kernel_tflops": 2.0 * N * M * M / (k64_ms / max(k64_n, 1) / 1e3) / 1e12 if k64_n else None,
+                    "steps": n_chk, "speedup_of_tensor_path": value / fp64_step,
+                    "note": "scatter_fp64_kernel (FP64 CUDA cores, tiled, W in shared memory) running the same "
+                            "relaxed source iteration on the same inputs; the tensor path's target is >= 5x"}
         S_64 = ctx.solve_read()
         r64 = ctx.solve_residual_history(n_chk).tolist()
         rel = np.abs(S_t - S_64) / np.abs(S_64)
@@ -632,6 +690,28 @@ def run_ours(args, rank, world, local):
         accuracy["eval_max_rel_err"] = float(rel.max())
         accuracy["eval_mean_rel_err"] = float(rel.mean())
         del S_t, S_64, rel
+
+    # the serving loop (configuration 5's request distribution) on a short
+    # stream: saturated throughput, the isolated latencies of the 0.8-load
+    # stream's requests and that stream's p50 / p99
+    serve = None
+    if rank == 0 and world == 1 and not args.no_serve:
+        import bench_configs as bc
+
+        sres = bc.config5(pkg, _native, ctx, torch, loads=(0.8,), window_s=args.serve_window, precision=prec)
+        row = sres["loads"][0]
+        serve = {"saturation_cell_dir_iter_per_s": sres["saturation_cell_dir_iter_per_s"],
+                 "load": row["offered_load"], "requests": row["requests"], "completed": row["completed"],
+                 "p50_ms": row["p50_ms"], "p99_ms": row["p99_ms"],
+                 "isolated_p50_ms": row.get("isolated_p50_ms"), "isolated_p99_ms": row.get("isolated_p99_ms"),
+                 "p99_over_isolated_p99": row.get("p99_vs_isolated_p99"),
+                 "mean_queue_ms": row.get("mean_queue_ms"), "p99_queue_ms": row.get("p99_queue_ms"),
+                 "throughput_cell_dir_iter_per_s": row["throughput_cell_dir_iter_per_s"],
+                 "policy": sres["policy"], "window_s": args.serve_window,
+                 "workload": "configuration 5's requests (cells lognormal median 50,000 clipped to [2k, 500k], "
+                             "M in {110, 302, 590, 1202}, HG g~U(0, 0.8), 5-40 iterations, FP32 lognormal(0,1)), "
+                             "Poisson arrivals rescaled to 0.8 of the saturated throughput, 120 GB HBM cap; "
+                             "latency counts from arrival (queueing included)"}
 
     # roofline of the dominant kernel
     peaks, src = load_peaks()
@@ -675,8 +755,9 @@ def run_ours(args, rank, world, local):
                    "accuracy_gate": "max rel err vs FP64 path <= 1e-6 after the timed steps (see accuracy)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (no flush)", "step": "integral + update + residual + relaxation"},
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-        "accuracy": accuracy, "residuals": residuals,
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "e2e_host_call": e2e_host_call,
+        "gpu_launches": launches, "clocks": clk, "accuracy": accuracy, "fp64_gpu": fp64_gpu, "serve": serve,
+        "residuals": residuals,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -135,18 +135,37 @@ int rts_copy_illum(rts_ctx* ctx, int64_t size, const double* illum_host);
 /* scattering integral (FP64, the drop-in path)                            */
 /* ---------------------------------------------------------------------- */
 
+/* Arithmetic of the reference-compatible integral calls rts_scattering_async
+ * and rts_scattering (rts_precision; RTS_PREC_FP64 by default, which matches
+ * the reference's CPU integral to 1e-12 relative).  A tensor precision runs
+ * the same calls on the tcgen05 split path (RTS_PREC_FP16X3 and
+ * RTS_PREC_TF32X3 to 1e-6 relative, RTS_PREC_BF16X3 to ~1e-5): the
+ * reference's kernel d_GetS_MPI_Stream at that precision, behind the same
+ * call.  RTS_ERR_UNSUPPORTED for a tensor precision on a device other than
+ * sm_10x. */
+int rts_set_precision(rts_ctx* ctx, int precision);
+int rts_get_precision(const rts_ctx* ctx, int* precision);
+
 /* Replaces CalculateIntScatteringAsyncMPIStream (cuda/cuda_solve.cu:89-111,
  * kernel d_GetS_MPI_Stream at cuda/cuda_kernel.cu:82-111): computes local
- * out-directions [start, end) on `stream` and queues the D2H of rows
+ * out-directions [start, end) of the device Illum on `stream`, at the
+ * context's precision (rts_set_precision), and queues the D2H of rows
  * [start, end) to host_out + start*N (host_out NULL: the pinned host
  * scattering array).  The reference offsets the copy by `start` elements,
- * which is right only for start == 0; this entry point uses start*N. */
+ * which is right only for start == 0; this entry point uses start*N.  Work on
+ * a stream other than RTS_STREAM_SCATTERING_1 is ordered after the Illum
+ * copies queued there.  Calls on different streams may overlap, as the
+ * reference's pair on scattering streams 1 and 2 does
+ * (solve_module/illum/Illum_async.cpp:1019-1020): at a tensor precision each
+ * stream slot has split operands of its own, and rows both calls cover
+ * receive the same values from either. */
 int rts_scattering_async(rts_ctx* ctx, int64_t start, int64_t end, int stream, double* host_out);
 
 /* Replaces CalculateIntScattering (cuda/cuda_solve.cu:153-170): copies
  * illum_host (all M*N*4 doubles; NULL: the pinned host Illum) to the device,
- * computes every local out-direction and copies the result to host_out
- * (NULL: the pinned host scattering array), synchronously. */
+ * computes every local out-direction at the context's precision and copies
+ * the result to host_out (NULL: the pinned host scattering array),
+ * synchronously. */
 int rts_scattering(rts_ctx* ctx, const double* illum_host, double* host_out);
 
 /* Copies rows [start, end) of the device scattering array to host_out +
@@ -172,21 +191,26 @@ int rts_send_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, co
 
 /* Allocation-free FP64 scattering integral.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory --
- * code that runs inside a caller-owned memory pool or arena, code called
- * while a stream is being captured into a CUDA graph (a cudaMalloc there would
- * break the capture), and hosts that budget every device byte up front.
- * The caller passes device pointers: Illum [M][N][4], directions xyz [M][3]
- * and area [M], and the output scattering [M][N] (all out-directions); the
- * work is queued on `stream` (a cudaStream_t, NULL for the default stream)
- * and nothing is synchronised or allocated -- no cudaMalloc, cudaFree or
- * allocating library call.  The only scratch, the M x M FP64 direction-pair
- * matrix, lives in a fixed 2 MB device array of the library that every GPU
- * loading the library holds until the process exits; hence the limit
- * M <= RTS_NOALLOC_MAX_DIRS (larger M returns RTS_ERR_INVALID_ARGUMENT).
- * The scratch is shared by all calls and rewritten in full by each: calls
- * that overlap on the GPU race.  The first call on a device looks the scratch
- * address up for that device (cudaGetSymbolAddress, with that device
- * current); make that first call before any stream capture. */
+ * code that runs inside a caller-owned memory pool or arena that forbids
+ * allocations outside it, and hosts that budget every device byte up front.
+ * The caller passes device pointers: Illum [M][N][4] (16-byte aligned: it is
+ * read as pairs of doubles), directions xyz [M][3] and area [M], and the
+ * output scattering [M][N] (all out-directions), the last three 8-byte
+ * aligned; a misaligned pointer returns RTS_ERR_INVALID_ARGUMENT before
+ * anything is launched.  The work is queued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and nothing is synchronised or allocated -- no
+ * cudaMalloc, cudaFree or allocating library call.  The only scratch, the
+ * M x M FP64 direction-pair matrix, lives in a fixed 2 MB device array of the
+ * library that every GPU loading the library holds until the process exits;
+ * hence the limit M <= RTS_NOALLOC_MAX_DIRS (larger M returns
+ * RTS_ERR_INVALID_ARGUMENT).  The scratch is shared by all calls and
+ * rewritten in full by each: calls that overlap on the GPU race.  Each call
+ * outside a stream capture looks the scratch address up for the current
+ * device (cudaGetSymbolAddress); a call made while its stream is being
+ * captured reuses the address of the last uncaptured call on that device, so
+ * make the first call on a device before any stream capture.  An error that
+ * the caller's own earlier work left pending is returned as RTS_ERR_CUDA
+ * without launching and is left pending. */
 #define RTS_NOALLOC_MAX_DIRS 512
 int rts_scattering_noalloc(const double* d_illum, const double* d_xyz, const double* d_area, int64_t N,
                            int64_t M, double full_area, double* d_scattering, void* stream);

@@ -26,7 +26,9 @@ BUILD_DIR = ORACLE_DIR / "_build"
 LIB_PATH = BUILD_DIR / "liborc.so"
 REF_DIR = ORACLE_DIR / "_ref"
 REF_LIB = REF_DIR / "libref_scatter.so"
-REFERENCE_ROOT = Path(os.environ.get("RTS_REFERENCE_ROOT", "/root/reference"))
+# The reference tree: RTS_REFERENCE_ROOT, else the directory "reference" beside
+# this repository's root (the development layout).  Absent on the GPU hosts.
+REFERENCE_ROOT = Path(os.environ.get("RTS_REFERENCE_ROOT") or (ORACLE_DIR.parent.parent / "reference"))
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

@@ -37,8 +37,9 @@
 #   solve_module/illum/Illum_async.cpp:172-199, 259-510, 726-784
 #       CalculateIllumeOnInnerFace, GetCurIllum, ReCalcIllum, the sweep loop
 set -eu
-REF=${RTS_REFERENCE_ROOT:-/root/reference}/solver_hllc_illum_cuda
 HERE=$(cd "$(dirname "$0")" && pwd)
+# the reference tree: RTS_REFERENCE_ROOT, else "reference" beside the repository root
+REF=${RTS_REFERENCE_ROOT:-$HERE/../../reference}/solver_hllc_illum_cuda
 OUT="$HERE/_ref"
 if [ ! -d "$REF" ]; then
     echo "reference tree not found at $REF; nothing to build" >&2

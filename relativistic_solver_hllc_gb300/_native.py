@@ -85,6 +85,8 @@ _SIGNATURES = {
     "rts_set_weights": (C.c_int, [_vp, _dp]),
     "rts_send_illum_async": (C.c_int, [_vp, _i64, _i64, _i64, _dp]),
     "rts_copy_illum": (C.c_int, [_vp, _i64, _dp]),
+    "rts_set_precision": (C.c_int, [_vp, C.c_int]),
+    "rts_get_precision": (C.c_int, [_vp, C.POINTER(C.c_int)]),
     "rts_scattering_async": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
     "rts_scattering": (C.c_int, [_vp, _dp, _dp]),
     "rts_read_scattering": (C.c_int, [_vp, _i64, _i64, C.c_int, _dp]),
@@ -427,6 +429,16 @@ class Context:
         self._check(self.lib.rts_copy_illum(self.h, int(size), _ptr(a)), "rts_copy_illum")
 
     # -- integrals --------------------------------------------------------
+    def set_precision(self, precision):
+        """Arithmetic of scattering_async / scattering ("fp64", "fp16x3", "bf16x3", "tf32x3")."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self._check(self.lib.rts_set_precision(self.h, prec), "rts_set_precision")
+
+    def get_precision(self) -> int:
+        v = C.c_int()
+        self._check(self.lib.rts_get_precision(self.h, C.byref(v)), "rts_get_precision")
+        return v.value
+
     def scattering_async(self, start: int, end: int, stream: int, out: np.ndarray | None = None):
         if out is not None:
             if out.dtype != np.float64 or not out.flags.c_contiguous:

@@ -25,10 +25,12 @@
 //
 // Precision: every call is FP64, bit-compatible with the reference, unless
 // the RTS_SCATTER_PRECISION environment variable names a tensor-core
-// precision (fp16x3, bf16x3 or tf32x3).  Then the synchronous
-// CalculateIntScattering (host Illum in, host scattering out) runs the split
-// tcgen05 path through rts_scattering_update, to <= 1e-6 relative for fp16x3
-// and tf32x3.  The asynchronous calls on the device-resident Illum stay FP64.
+// precision (fp16x3, bf16x3 or tf32x3).  Then InitDevice sets that precision
+// on the context (rts_set_precision) and every scattering call -- the
+// asynchronous calls on the device-resident Illum that the source iteration
+// makes (CalculateIntScatteringAsyncMPIStream, ...AsyncMPI, ...Async) and the
+// synchronous CalculateIntScattering -- runs the split tcgen05 path, to
+// <= 1e-6 relative for fp16x3 and tf32x3.
 //
 // Cell geometry: like the reference's InitDevice (cuda/cuda_struct.cu:134-176),
 // the first rank reads normals.bin, squares.bin and volume.bin from the
@@ -55,7 +57,7 @@ int g_device = 0;
 bool g_owns_moments = false;
 
 // RTS_SCATTER_PRECISION: fp64 (default), fp16x3, bf16x3 or tf32x3
-int sync_precision()
+int env_precision()
 {
     const char* v = std::getenv("RTS_SCATTER_PRECISION");
     if (!v) return RTS_PREC_FP64;
@@ -152,6 +154,7 @@ void InitDevice(const grid_directions_t& grid_dir_host, grid_t& grid_host, const
         return;
     rts_host_illum(g_ctx, &grid_host.Illum);
     rts_host_scattering(g_ctx, &grid_host.scattering);
+    report(rts_set_precision(g_ctx, env_precision()), "InitDevice (precision)");
     if (start == 0) {  // the first rank also receives the moments (cuda/cuda_struct.cu:158-175)
         grid_host.divstream = new Type[grid_host.size]();
         grid_host.divimpuls = new Vector3[grid_host.size]();
@@ -241,10 +244,6 @@ int CalculateIntScatteringAsync(const grid_directions_t& grid_dir, grid_t& grid)
 
 int CalculateIntScattering(const grid_directions_t&, grid_t& grid)
 {
-    const int prec = sync_precision();
-    if (prec != RTS_PREC_FP64)  // lambda = 1: the bare integral at that precision
-        return report(rts_scattering_update(g_ctx, prec, grid.Illum, nullptr, 1.0, grid.scattering),
-                      "CalculateIntScattering");
     return report(rts_scattering(g_ctx, grid.Illum, grid.scattering), "CalculateIntScattering");
 }
 

@@ -121,6 +121,20 @@ static void free_grid(rts_ctx* ctx)
 
 static bool valid_stream(int s) { return s >= 0 && s < RTS_STREAM_COUNT; }
 
+// Orders stream slot `stream` after the work already queued on the
+// scattering stream (where the Illum copies go), with the context's event of
+// that slot: recording and waiting capture the event's state at the call, so
+// one event per waiting stream is enough.
+static int after_scattering_stream(rts_ctx* ctx, int stream)
+{
+    if (stream == RTS_STREAM_SCATTERING_1) return RTS_OK;
+    cudaEvent_t& ev = ctx->ev_order[stream];
+    if (!ev) RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RTS_CUDA_TRY(ctx, cudaEventRecord(ev, ctx->streams[RTS_STREAM_SCATTERING_1]));
+    RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->streams[stream], ev, 0));
+    return RTS_OK;
+}
+
 void rts_timing_begin(rts_ctx* ctx, cudaStream_t st)
 {
     if (!ctx->timing) return;
@@ -226,6 +240,10 @@ int rts_ctx_destroy(rts_ctx* ctx)
     for (int i = 0; i < RTS_STREAM_COUNT; ++i)
         if (ctx->streams[i]) cudaStreamDestroy(ctx->streams[i]);
     for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
+    for (int i = 0; i < RTS_STREAM_COUNT; ++i) {
+        if (ctx->ev_order[i]) cudaEventDestroy(ctx->ev_order[i]);
+        if (ctx->ev_sync[i]) cudaEventDestroy(ctx->ev_sync[i]);
+    }
     delete ctx;
     return RTS_OK;
 }
@@ -409,14 +427,12 @@ int rts_scattering_async(rts_ctx* ctx, int64_t start, int64_t end, int stream, d
     if (start == end) return RTS_OK;
     cudaStream_t st = ctx->streams[stream];
     // Illum copies go on stream 0; a later stream must see them.
-    if (stream != RTS_STREAM_SCATTERING_1) {
-        cudaEvent_t ev;
-        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        cudaEventRecord(ev, ctx->streams[RTS_STREAM_SCATTERING_1]);
-        cudaStreamWaitEvent(st, ev, 0);
-        cudaEventDestroy(ev);
-    }
-    int rc = rts_launch_scatter_fp64(ctx, start, end, st, nullptr, 0.0, false, false);
+    int rc = after_scattering_stream(ctx, stream);
+    if (rc != RTS_OK) return rc;
+    if (ctx->call_precision == RTS_PREC_FP64)
+        rc = rts_launch_scatter_fp64(ctx, start, end, st, nullptr, 0.0, false, false);
+    else
+        rc = rts_split_async(ctx, ctx->call_precision, start, end, stream, st);
     if (rc != RTS_OK) return rc;
     double* dst = host_out ? host_out : ctx->h_S;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(dst + start * ctx->N, ctx->d_S + start * ctx->N,
@@ -430,13 +446,17 @@ int rts_scattering(rts_ctx* ctx, const double* illum_host, double* host_out)
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     RTS_REQUIRE(ctx, ctx->d_S, RTS_ERR_BAD_STATE, "rts_scattering before rts_init");
     const double* src = illum_host ? illum_host : ctx->h_illum;
+    double* dst = host_out ? host_out : ctx->h_S;
+    if (ctx->call_precision != RTS_PREC_FP64) {  // the bare integral at that precision, pipelined over cell ranges
+        ctx->solve_ready = false;
+        return rts_split_host_call(ctx, ctx->call_precision, src, nullptr, 1.0, dst);
+    }
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_illum, src, rts_bytes<double>(ctx->M * ctx->N * 4),
                                       cudaMemcpyHostToDevice, st));
     ctx->solve_ready = false;
     int rc = rts_launch_scatter_fp64(ctx, 0, ctx->local(), st, nullptr, 0.0, false, false);
     if (rc != RTS_OK) return rc;
-    double* dst = host_out ? host_out : ctx->h_S;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(dst, ctx->d_S, rts_bytes<double>(ctx->local() * ctx->N),
                                       cudaMemcpyDeviceToHost, st));
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -521,14 +541,9 @@ int rts_moments(rts_ctx* ctx, int stream, double* energy, double* flux)
     RTS_REQUIRE(ctx, ctx->d_illum, RTS_ERR_BAD_STATE, "rts_moments before rts_init");
     RTS_REQUIRE(ctx, valid_stream(stream), RTS_ERR_INVALID_ARGUMENT, "bad stream id %d", stream);
     cudaStream_t st = ctx->streams[stream];
-    if (stream != RTS_STREAM_SCATTERING_1) {
-        cudaEvent_t ev;
-        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        cudaEventRecord(ev, ctx->streams[RTS_STREAM_SCATTERING_1]);
-        cudaStreamWaitEvent(st, ev, 0);
-        cudaEventDestroy(ev);
-    }
-    int rc = rts_launch_moments(ctx, st);
+    int rc = after_scattering_stream(ctx, stream);
+    if (rc != RTS_OK) return rc;
+    rc = rts_launch_moments(ctx, st);
     if (rc != RTS_OK) return rc;
     if (energy)
         RTS_CUDA_TRY(ctx, cudaMemcpyAsync(energy, ctx->d_energy, rts_bytes<double>(ctx->N),
@@ -580,14 +595,9 @@ int rts_illum_params(rts_ctx* ctx, int stream, double* energy, double* flux, dou
         ctx->d_params = (double*)p;
     }
     cudaStream_t st = ctx->streams[stream];
-    if (stream != RTS_STREAM_SCATTERING_1) {  // after the Illum copies queued on the scattering stream
-        cudaEvent_t ev;
-        RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        cudaEventRecord(ev, ctx->streams[RTS_STREAM_SCATTERING_1]);
-        cudaStreamWaitEvent(st, ev, 0);
-        cudaEventDestroy(ev);
-    }
-    int rc = rts_launch_illum_params(ctx, st);
+    int rc = after_scattering_stream(ctx, stream);  // after the Illum copies queued on the scattering stream
+    if (rc != RTS_OK) return rc;
+    rc = rts_launch_illum_params(ctx, st);
     if (rc != RTS_OK) return rc;
     double* const d = ctx->d_params;
     struct {
@@ -657,12 +667,10 @@ int rts_sync_stream(rts_ctx* ctx, int stream, int64_t timeout_us)
 {
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     RTS_REQUIRE(ctx, valid_stream(stream), RTS_ERR_INVALID_ARGUMENT, "bad stream id %d", stream);
-    cudaEvent_t ev;
-    RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    cudaEventRecord(ev, ctx->streams[stream]);
-    int rc = wait_event_deadline(ctx, ev, timeout_us);
-    cudaEventDestroy(ev);
-    return rc;
+    cudaEvent_t& ev = ctx->ev_sync[stream];
+    if (!ev) RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RTS_CUDA_TRY(ctx, cudaEventRecord(ev, ctx->streams[stream]));
+    return wait_event_deadline(ctx, ev, timeout_us);
 }
 
 int rts_wait(rts_ctx* ctx, int64_t timeout_us)
@@ -853,6 +861,27 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
     default:
         return rts_fail(ctx, RTS_ERR_INVALID_ARGUMENT, "unknown tuning key %d", key);
     }
+}
+
+int rts_set_precision(rts_ctx* ctx, int precision)
+{
+    if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
+    RTS_REQUIRE(ctx,
+                precision == RTS_PREC_FP64 || precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3 ||
+                    precision == RTS_PREC_TF32X3,
+                RTS_ERR_INVALID_ARGUMENT, "rts_set_precision: unknown precision %d", precision);
+    RTS_REQUIRE(ctx, precision == RTS_PREC_FP64 || ctx->cc_major == 10, RTS_ERR_UNSUPPORTED,
+                "the tensor-core precisions need a Blackwell (sm_10x) device, found sm_%d%d", ctx->cc_major,
+                ctx->cc_minor);
+    ctx->call_precision = precision;
+    return RTS_OK;
+}
+
+int rts_get_precision(const rts_ctx* ctx, int* precision)
+{
+    if (!ctx || !precision) return RTS_ERR_INVALID_ARGUMENT;
+    *precision = ctx->call_precision;
+    return RTS_OK;
 }
 
 int rts_stream_handle(rts_ctx* ctx, int stream, void** handle)

@@ -515,12 +515,11 @@ int rts_launch_synth(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int i
 //
 // For callers that cannot allocate device memory themselves or through us:
 // code running under a caller-owned memory pool or arena that forbids
-// allocations outside it, code called while a stream is being captured
-// (where cudaMalloc would break the capture), and hosts that account every
-// device byte up front.  The caller passes device inputs and outputs; the only
-// scratch -- the M x M FP64 direction-pair matrix W -- lives in the
-// file-scope array below, which every GPU that loads this library holds
-// until the process exits.
+// allocations outside it, and hosts that account every device byte up
+// front.  The caller passes device inputs and outputs; the only scratch --
+// the M x M FP64 direction-pair matrix W -- lives in the file-scope array
+// below, which every GPU that loads this library holds until the process
+// exits.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -530,22 +529,32 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 double* g_noalloc_w_addr[NOALLOC_MAX_DEVICES] = {};
 std::mutex g_noalloc_mutex;
 
-// Device address of the scratch array, looked up once per device with that
-// device current (host code cannot use the symbol itself as a pointer).
-double* noalloc_scratch(int device)
+// Device address of the scratch array for `device` (current).  Host code
+// cannot use the symbol itself as a pointer, so the address is looked up with
+// cudaGetSymbolAddress.  Outside a stream capture it is looked up on every
+// call, so a module reloaded after a device reset is seen at its new address;
+// the last address found is kept for calls made while `st` is being captured,
+// which must therefore follow an uncaptured call on the same device.
+double* noalloc_scratch(int device, cudaStream_t st)
 {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES) return nullptr;
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_w_addr[device]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_w) != cudaSuccess) {
-            cudaGetLastError();
-            return nullptr;
-        }
-        g_noalloc_w_addr[device] = static_cast<double*>(p);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
     }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (cap != cudaStreamCaptureStatusNone) return g_noalloc_w_addr[device];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_w) != cudaSuccess) {
+        cudaGetLastError();  // our own lookup's error; none was pending on entry
+        return nullptr;
+    }
+    g_noalloc_w_addr[device] = static_cast<double*>(p);
     return g_noalloc_w_addr[device];
 }
+
+bool aligned(const void* p, uintptr_t bytes) { return (reinterpret_cast<uintptr_t>(p) & (bytes - 1)) == 0; }
 
 }  // namespace
 
@@ -556,21 +565,27 @@ extern "C" int rts_scattering_noalloc(const double* d_illum, const double* d_xyz
     if (!d_illum || !d_xyz || !d_area || !d_scattering) return RTS_ERR_INVALID_ARGUMENT;
     if (N <= 0 || M <= 0 || !(full_area > 0.0)) return RTS_ERR_INVALID_ARGUMENT;
     if (M > RTS_NOALLOC_MAX_DIRS) return RTS_ERR_INVALID_ARGUMENT;  // the scratch holds M <= 512
+    // Illum is read as pairs of doubles (16-byte loads); the rest as doubles
+    if (!aligned(d_illum, 16) || !aligned(d_xyz, 8) || !aligned(d_area, 8) || !aligned(d_scattering, 8))
+        return RTS_ERR_INVALID_ARGUMENT;
     const int64_t gx = (N + F64_TC - 1) / F64_TC;
     if (gx >= (1ll << 31)) return RTS_ERR_INVALID_ARGUMENT;
+    // An error left pending by the caller's own earlier work is theirs: report
+    // it without launching and without clearing it.
+    if (cudaPeekAtLastError() != cudaSuccess) return RTS_ERR_CUDA;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) {
         cudaGetLastError();
         return RTS_ERR_CUDA;
     }
-    double* W = noalloc_scratch(device);
-    if (!W) return RTS_ERR_CUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double* W = noalloc_scratch(device, st);
+    if (!W) return RTS_ERR_CUDA;
     // W is rewritten in full (all M x M entries) by every call: nothing in the
     // scratch has to start at zero, and calls that overlap on the GPU race.
     weights_kernel<<<(unsigned)((M + 127) / 128), 128, 0, st>>>(d_xyz, d_area, (int)M, 0, (int)M, full_area,
                                                                 RTS_PHASE_THOMSON, 0.0, W);
-    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;  // nothing was pending: this launch's error
     dim3 grid((unsigned)gx, (unsigned)((M + F64_TK - 1) / F64_TK));
     scatter_fp64_kernel<false, false><<<grid, F64_THREADS, 0, st>>>(d_illum, W, N, (int)M, (int)M, 0, (int)M,
                                                                      d_scattering, nullptr, 0.0, nullptr);

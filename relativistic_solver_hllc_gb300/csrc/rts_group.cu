@@ -289,7 +289,7 @@ void rts_group_batch_free(rts_batch* b)
 {
     if (!b) return;
     rts_ctx* ctx = b->ctx;
-    cudaStreamSynchronize(ctx->streams[RTS_STREAM_SCATTERING_1]);
+    for (int i = 0; i < RTS_STREAM_COUNT; ++i) cudaStreamSynchronize(ctx->streams[i]);  // a batch may run on any slot
     drop_graph(b);
     for (GProb* p : b->probs) free_prob(ctx, p);
     rts_dfree(ctx, b->d_table, b->table_cap * sizeof(GroupProblem));

@@ -62,6 +62,15 @@ struct rts_split_state {
     int64_t chunk_w_version[RTS_HOST_CHUNKS] = {};
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t ev_start = nullptr, ev_in[RTS_HOST_CHUNKS] = {}, ev_done[RTS_HOST_CHUNKS] = {};
+    // reference-compatible asynchronous calls (rts_scattering_async) at a
+    // tensor precision: one one-problem batch per stream slot, each with its
+    // own split operands, so that calls queued on different streams at the
+    // same time (the reference's pair on scattering streams 1 and 2) never
+    // share a buffer they write
+    rts_batch* slot[RTS_STREAM_COUNT] = {};
+    int64_t slot_id[RTS_STREAM_COUNT] = {};
+    int64_t slot_start[RTS_STREAM_COUNT] = {};
+    int64_t slot_w_version[RTS_STREAM_COUNT] = {};
 };
 
 // Device state of the transport sweep (rts_sweep.cu): the mesh, the
@@ -155,6 +164,9 @@ struct rts_ctx {
     bool solve_ready = false;
     bool solve_has_prev = false;
     int64_t solve_steps = 0;
+    int call_precision = RTS_PREC_FP64;  // rts_scattering_async / rts_scattering (rts_set_precision)
+    cudaEvent_t ev_order[RTS_STREAM_COUNT] = {};  // cross-stream ordering, one per waiting stream
+    cudaEvent_t ev_sync[RTS_STREAM_COUNT] = {};   // rts_sync_stream deadlines
     rts_split_state split;
     int split_flush = 0;         // hi*hi drain period in stages (0: default)
     int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
@@ -228,6 +240,10 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
 // One evaluation from the device Illum (faces) into the FP64 device S for
 // every local out-direction, no host copies (the sweep's source iteration).
 int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st);
+// Local out-directions [start, end) from the device Illum (faces) into rows
+// [start, end) of the FP64 device S on `st`, with the split operands of
+// stream slot `slot` (no host copies, no host synchronisation once set up).
+int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int slot, cudaStream_t st);
 int rts_split_read(rts_ctx* ctx, double* S_host);
 int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host);
 void rts_split_free(rts_ctx* ctx);

@@ -260,6 +260,61 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     return RTS_OK;
 }
 
+// rts_scattering_async at a tensor precision: local out-directions
+// [start, end) of the device Illum into rows [start, end) of the FP64 device
+// S, on `st`.  Stream slot `slot` keeps its own one-problem batch (split
+// Ibar rows, row scales, the split W columns [start, end), table, residual),
+// rebuilt when the range, shape, precision or flush period changes and its W
+// split again when the context's W changed.  Two calls queued on different
+// slots at once -- the reference's pair [0, size_1) on scattering stream 1
+// and [0, local) on scattering stream 2 -- therefore write no common buffer
+// except the rows of S they share, into which both write the same values
+// (each output's arithmetic does not depend on the tiling of the
+// out-directions).  After the first call of a slot nothing synchronises the
+// host.
+int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int slot, cudaStream_t st)
+{
+    RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
+    RTS_REQUIRE(ctx, slot >= 0 && slot < RTS_STREAM_COUNT, RTS_ERR_INVALID_ARGUMENT, "bad stream slot %d", slot);
+    rts_split_state& s = ctx->split;
+    const int mode = rts_split_mode(precision);
+    const int64_t N = ctx->N, M = ctx->M, loc = ctx->local(), Mout = end - start;
+    const int flush = ctx->split_flush > 0 ? ctx->split_flush : 1;
+    int rc;
+    GProb* p = s.slot[slot] ? rts_group_find(s.slot[slot], s.slot_id[slot], nullptr) : nullptr;
+    if (p && (p->mode != mode || p->N != N || p->M != M || p->Mout != Mout || p->flush != flush ||
+              s.slot_start[slot] != start)) {
+        if ((rc = rts_group_remove_on(s.slot[slot], s.slot_id[slot], st)) != RTS_OK) return rc;
+        p = nullptr;
+    }
+    if (!s.slot[slot] && (rc = rts_group_batch_new(ctx, &s.slot[slot])) != RTS_OK) return rc;
+    if (!p) {
+        rc = rts_group_new_problem(s.slot[slot], N, M, Mout, 1, ctx->d_W + start, (int)loc, mode, flush, 0, false, &p,
+                                   st);
+        if (rc != RTS_OK) return rc;
+        if ((rc = rts_group_attach(s.slot[slot], p, &s.slot_id[slot])) != RTS_OK) return rc;
+        s.slot_start[slot] = start;
+        s.slot_w_version[slot] = ctx->w_version;
+    } else if (s.slot_w_version[slot] != ctx->w_version) {
+        rc = rts_pp_split_w(ctx, ctx->d_W + start, (int)M, (int)Mout, (int)loc, (int)p->kpad, (int)p->mpad, mode, p->wc,
+                            p->cs, st);
+        if (rc != RTS_OK) return rc;
+        s.slot_w_version[slot] = ctx->w_version;
+    }
+    double* const S64 = ctx->d_S + start * N;
+    if (p->S64 != S64 || p->ldS != N || p->use_B || p->cur != 0) {
+        p->cur = 0;
+        p->S64 = S64;
+        p->ldS = N;
+        p->use_B = false;
+        rts_group_invalidate(s.slot[slot]);
+    }
+    rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)M, (int)p->kpad, nullptr, mode, p->rs, p->rows_pad,
+                                p->a[0], st);
+    if (rc != RTS_OK) return rc;
+    return rts_group_step(s.slot[slot], 0, st);
+}
+
 int rts_split_read(rts_ctx* ctx, double* S_host)
 {
     RTS_REQUIRE(ctx, ctx->split.iter, RTS_ERR_BAD_STATE, "no tensor-path source iteration set up");
@@ -296,6 +351,7 @@ void rts_split_free(rts_ctx* ctx)
 {
     rts_split_state& s = ctx->split;
     rts_group_batch_free(s.iter);
+    for (int i = 0; i < RTS_STREAM_COUNT; ++i) rts_group_batch_free(s.slot[i]);
     for (int i = 0; i < RTS_HOST_CHUNKS; ++i) {
         rts_group_batch_free(s.chunk[i]);
         if (s.ev_in[i]) cudaEventDestroy(s.ev_in[i]);

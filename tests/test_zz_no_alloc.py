@@ -1,12 +1,12 @@
 """The allocation-free entry point rts_scattering_noalloc.
 
 Callers that cannot allocate device memory -- code inside a caller-owned
-memory pool, code running while a stream is captured into a CUDA graph, hosts
-that budget every device byte -- pass their own device buffers; the library's
-only scratch is a fixed device array.  This test calls the entry point through
-the C ABI twice in a row, with different problem sizes, and checks each result
-against the context-based entry point rts_scattering on the same inputs,
-within the FP64 tolerance of the other parity tests (1e-12 relative).
+memory pool or arena, hosts that budget every device byte -- pass their own
+device buffers; the library's only scratch is a fixed device array.  This
+test calls the entry point through the C ABI twice in a row, with different
+problem sizes, and checks each result against the context-based entry point
+rts_scattering on the same inputs, within the FP64 tolerance of the other
+parity tests (1e-12 relative).
 
 Kept in a file of its own, collected last, so that a run that stops at the
 first failure has run every other test first.
@@ -67,3 +67,7 @@ def test_noalloc_rejects_oversized_direction_sets(native_lib):
     p = buf.data_ptr()
     assert fn(p, p, p, 1, 513, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
     assert fn(None, p, p, 1, 4, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
+    # Illum is read as pairs of doubles: an 8-byte offset view is refused
+    # before anything is launched, as is a misaligned output
+    assert fn(p + 8, p, p, 1, 4, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
+    assert fn(p, p, p, 1, 4, 1.0, p + 4, None) == _native.ERR_INVALID_ARGUMENT
