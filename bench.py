@@ -713,6 +713,22 @@ def run_ours(args, rank, world, local):
                              "Poisson arrivals rescaled to 0.8 of the saturated throughput, 120 GB HBM cap; "
                              "latency counts from arrival (queueing included)"}
 
+    # measured ceilings of this machine for the FP64 kernel and the host link
+    # (FMA chains on every SM; 1 GiB pinned copies each way and both at once)
+    measured = {"fp64_tflops": ctx.measure_fp64_peak(2.0), "link": ctx.measure_link(1 << 30, 5)}
+    lk = measured["link"]
+    for leg in (e2e, e2e_host_call):
+        moved = leg["h2d_bytes_per_step"] + leg["d2h_bytes_per_step"]
+        leg["link_gbs"] = moved / (leg["ms_per_step"] / 1e3) / 1e9
+        # the copies of one step at the measured rates, H2D and D2H overlapped
+        floor_s = max(leg["h2d_bytes_per_step"] / (lk["h2d_gbs"] * 1e9), leg["d2h_bytes_per_step"] / (lk["d2h_gbs"] * 1e9),
+                      moved / (lk["bidirectional_gbs"] * 1e9))
+        leg["link_floor_ms"] = floor_s * 1e3
+        leg["link_frac"] = floor_s / (leg["ms_per_step"] / 1e3)
+    if fp64_gpu and fp64_gpu.get("kernel_tflops"):
+        fp64_gpu["fp64_peak_tflops"] = measured["fp64_tflops"]
+        fp64_gpu["roofline_frac"] = fp64_gpu["kernel_tflops"] / measured["fp64_tflops"]
+
     # roofline of the dominant kernel
     peaks, src = load_peaks()
     flops = 2.0 * N * M * M
@@ -757,7 +773,7 @@ def run_ours(args, rank, world, local):
                    "l2": "inputs larger than L2 (no flush)", "step": "integral + update + residual + relaxation"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "e2e_host_call": e2e_host_call,
         "gpu_launches": launches, "clocks": clk, "accuracy": accuracy, "fp64_gpu": fp64_gpu, "serve": serve,
-        "residuals": residuals,
+        "measured_peaks": measured, "residuals": residuals,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -634,6 +634,16 @@ int rts_stream_handle(rts_ctx* ctx, int stream, void** handle);
  * *max_ulp receives the largest difference in units in the last place. */
 int rts_sweep_exp_check(rts_ctx* ctx, int64_t n, double* max_ulp);
 
+/* Measured ceilings for roofline fractions (no counterpart in the
+ * reference).  rts_measure_fp64_peak: FP64 FMA throughput of the device in
+ * TFLOP/s (2 flops per FMA), from independent FMA chains on every SM timed
+ * with CUDA events over about `seconds`.  rts_measure_link: pinned host <->
+ * device copy rates in GB/s for copies of `bytes`, best of `reps`: H2D alone,
+ * D2H alone, and both directions at once (bytes moved both ways / time).
+ * Each allocates its buffers for the duration of the call. */
+int rts_measure_fp64_peak(rts_ctx* ctx, double seconds, double* tflops);
+int rts_measure_link(rts_ctx* ctx, int64_t bytes, int reps, double* h2d_gbs, double* d2h_gbs, double* both_gbs);
+
 /* Number of kernels this context has launched so far. */
 int rts_launch_count(const rts_ctx* ctx, int64_t* count);
 

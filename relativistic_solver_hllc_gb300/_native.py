@@ -123,6 +123,8 @@ _SIGNATURES = {
     "rts_autotune_load": (C.c_int, [_vp, C.c_char_p]),
     "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "rts_launch_count": (C.c_int, [_vp, C.POINTER(_i64)]),
+    "rts_measure_fp64_peak": (C.c_int, [_vp, C.c_double, _dp]),
+    "rts_measure_link": (C.c_int, [_vp, _i64, C.c_int, _dp, _dp, _dp]),
     "rts_kernel_timing": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(_i64)]),
     "rts_mesh_cube": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _vp, _dp]),
     "rts_sweep_set_mesh": (C.c_int, [_vp, _dp, _vp, _dp]),
@@ -609,6 +611,19 @@ class Context:
         v = _vp()
         self._check(self.lib.rts_stream_handle(self.h, int(stream), C.byref(v)), "rts_stream_handle")
         return int(v.value or 0)
+
+    def measure_fp64_peak(self, seconds: float = 2.0) -> float:
+        """FP64 FMA throughput of the device, TFLOP/s."""
+        v = C.c_double()
+        self._check(self.lib.rts_measure_fp64_peak(self.h, float(seconds), C.byref(v)), "rts_measure_fp64_peak")
+        return v.value
+
+    def measure_link(self, nbytes: int = 1 << 30, reps: int = 5) -> dict:
+        """Pinned host <-> device copy rates, GB/s."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.rts_measure_link(self.h, int(nbytes), int(reps), C.byref(a), C.byref(b), C.byref(c)),
+                    "rts_measure_link")
+        return {"h2d_gbs": a.value, "d2h_gbs": b.value, "bidirectional_gbs": c.value, "bytes": int(nbytes)}
 
     def launch_count(self) -> int:
         v = _i64()

@@ -108,6 +108,9 @@ void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
     rts_pfree(ctx, p->B, (size_t)(p->rows * 4), st);
     rts_pfree(ctx, p->lam, (size_t)(p->groups * 4), st);
     rts_pfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4), st);
+    rts_pfree(ctx, p->vrow, (size_t)(p->kpad * 4), st);
+    rts_pfree(ctx, p->part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), st);
+    rts_pfree(ctx, p->delta, (size_t)(p->rows_pad * 4), st);
     delete p;
 }
 
@@ -133,33 +136,23 @@ int ensure_scratch(rts_batch* b, size_t bytes, cudaStream_t st)
 
 }  // namespace
 
-// Relative correction of the tensor core's truncating accumulation.  Each
-// FP32 accumulate inside tcgen05.mma rounds toward zero, so a chunk sum of
-// `flush` K-slices (4*flush cross-product MMAs, then 2*flush hi*hi MMAs) comes
-// out low by a roughly fixed fraction of itself: about 0.5 ulp per
-// truncating accumulate, and an ulp is 2^-24..2^-23 of the value.  Summed
-// over the chunks of an output the loss is close to that fraction of the
-// output, so scaling the output by (1 + it) removes most of the mean error.
-// The fraction depends on where the chunk sums fall inside their binades
-// (measured on GB300 against the FP64 path, Thomson and Henyey-Greenstein
-// kernels, M from 146 to 1000: 0.9e-7..1.2e-7 for FP16 at flush 1 on rough
-// lognormal intensities, ~0.75e-7 on the smoother iterates of a relaxed
-// source iteration); the table takes a value between the two.  Without it
-// the loss compounds through a relaxed iteration (1.3e-6 after 20 steps on
-// 663,552 x 1000); with it the error stays near the single-evaluation level.
-float rts_group_bias(const rts_ctx* ctx, int mode, int flush)
+// Constant relative correction of the tensor core's truncating FP32
+// accumulation, applied to every finished sum: none unless the caller sets
+// one (RTS_TUNE_BIAS n > 0: n * 1e-10).  Each accumulate inside tcgen05.mma
+// rounds toward zero, so sums come out low by ~1e-7 of themselves; how much
+// depends on how the partial sums grow inside each MMA, i.e. on the data.
+// Relaxed iterations, where the loss would compound, correct each cell from
+// the conserved sum of its integrals instead (rts_group_kernel.cuh); a single
+// evaluation keeps the loss of one pass.
+float rts_group_bias(const rts_ctx* ctx, int, int)
 {
-    if (ctx->split_bias < 0) return 0.0f;
     if (ctx->split_bias > 0) return (float)(ctx->split_bias * 1e-10);
-    // mean relative loss of one evaluation, between the first evaluation of
-    // rough (lognormal sigma 1..1.5) intensities and the smoother iterates of
-    // a relaxed source iteration
-    static const float table[3][2] = {
-        {6.0e-8f, 8.0e-8f},  // BF16 hi/lo, flush 1 / 2
-        {9.0e-8f, 1.8e-7f},  // FP16 hi/lo, flush 1 / 2
-        {7.5e-8f, 1.1e-7f},  // TF32 hi/lo, flush 1 / 2 (zero mean error over 20 relaxed steps, config 2)
-    };
-    return table[mode < 0 || mode > 2 ? 1 : mode][flush >= 2 ? 1 : 0];
+    return 0.0f;
+}
+
+int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles)
+{
+    return kpad * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 4;
 }
 
 // Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
@@ -189,7 +182,7 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
     const int64_t units = (mode == 2 ? 4 : 2) * kpad;
     int64_t bytes = mpad * units * 2 + 2 * mpad * 4 + 2 * rows_pad * 4 + rows * 4 + groups * 4;
     bytes += (iterative ? 2 : 1) * rows_pad * units * 2;
-    if (iterative) bytes += rows * M * 4;
+    if (iterative) bytes += rows * M * 4 + rts_group_energy_bytes(kpad, rows_pad, nt);
     return bytes;
 }
 
@@ -234,14 +227,22 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     GP_ALLOC(rs, (size_t)(2 * p->rows_pad * 4), "Ibar row scales");
     GP_ALLOC(B, (size_t)(p->rows * 4), "source B");
     GP_ALLOC(lam, (size_t)(p->groups * 4), "albedo");
+    const bool energy = iterative && Mout == Min;
     if (iterative) {
         GP_ALLOC(S32, (size_t)(p->rows * p->Mout * 4), "FP32 scattering");
+    }
+    if (energy) {
+        GP_ALLOC(vrow, (size_t)(p->kpad * 4), "W row sums");
+        GP_ALLOC(part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), "energy partial sums");
+        GP_ALLOC(delta, (size_t)(p->rows_pad * 4), "energy corrections");
     }
 #undef GP_ALLOC
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
     if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
     rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs, st);
+    if (rc == RTS_OK && p->vrow) rc = rts_pp_row_sums(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, p->vrow, st);
+    if (rc == RTS_OK && p->delta) rc = rts_group_reset_energy(ctx, p, st);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->units, p->bn);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->units, G_BM);
     if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->units, G_BM);
@@ -254,6 +255,13 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (!p->a[1]) memcpy(p->maps[1], p->maps[0], 128);
     if (!p->a[1]) memcpy(p->rmaps[1], p->rmaps[0], 128);
     *out = p;
+    return RTS_OK;
+}
+
+int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st)
+{
+    if (!p->delta) return RTS_OK;
+    RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->delta, 0, (size_t)(p->rows_pad * 4), st));
     return RTS_OK;
 }
 
@@ -352,6 +360,11 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.a[0] = p->a[0];
     g.a[1] = p->a[1] ? p->a[1] : p->a[0];
     g.resid = b->d_resid + i;
+    // RTS_TUNE_BIAS -1 switches the conservation-based correction off
+    const bool energy = p->part != nullptr && ctx->split_bias >= 0;
+    g.vrow = energy ? p->vrow : nullptr;
+    g.part = energy ? p->part : nullptr;
+    g.delta = energy ? p->delta : nullptr;
     p->slot = (int)i;
     tiles += p->m_tiles * p->n_tiles;
 }
@@ -422,6 +435,12 @@ static int enqueue_step(rts_batch* b, int relax, cudaStream_t st, int n)
         ctx->launches++;
     }
     if (relax) {
+        // each cell's correction of the next step (problems without the
+        // buffers return at once), then the buffer flip
+        const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * ctx->num_sms, 1 << 12));
+        group_energy_kernel<<<dim3(gx, (unsigned)n), 256, 0, st>>>(b->d_table, n);
+        RTS_CHECK_LAUNCH(ctx, "group_energy_kernel");
+        ctx->launches++;
         group_flip_kernel<<<(n + 127) / 128, 128, 0, st>>>(b->d_table, n);
         RTS_CHECK_LAUNCH(ctx, "group_flip_kernel");
         ctx->launches++;

@@ -34,6 +34,10 @@ struct GProb {
     int cur = 0;
     int slot = -1;           // index of the problem's residual in the last launched table
     size_t bytes = 0;
+    // energy-conservation correction of relaxed steps (iterative problems)
+    float* vrow = nullptr;   // [kpad] v_j = sum_k W[j][k]
+    double* part = nullptr;  // [n_tiles * 4][rows_pad][2] per-slot partial sums of a step
+    float* delta = nullptr;  // [rows_pad] per-row correction of the next step
     alignas(64) unsigned char maps[3][128];
     alignas(64) unsigned char rmaps[2][128];  // relaxation boxes of a[0], a[1]
 };
@@ -74,3 +78,7 @@ rts_ctx* rts_group_ctx(rts_batch* b);
 // caller changed cur / S64 / use_B of a problem) and drops a captured graph.
 void rts_group_invalidate(rts_batch* b);
 float rts_group_bias(const rts_ctx* ctx, int mode, int flush);
+// Bytes of the energy-correction buffers of an iterative problem.
+int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles);
+// Clears the per-row corrections (a restarted iteration starts uncorrected).
+int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st);

@@ -36,6 +36,20 @@
 // hi*hi products last: the truncation then costs about one FP32 ulp of the
 // chunk sum per hi*hi MMA.
 //
+// Relaxed source iterations correct the truncation of the FP32 accumulate
+// (each tcgen05.mma rounds toward zero, so the sums come out low by ~1e-7,
+// by an amount that depends on how the partial sums grow inside an MMA) with
+// a conserved quantity instead of a measured constant: for any W,
+//     sum_k (W^T I)_k = sum_j v_j I_j,    v_j = sum_k W[j][k]  (FP64, once).
+// Every relaxed step writes, per cell and per epilogue warp, the two partial
+// sums -- of the raw integrals it produced and of v_j times the split
+// intensities it read (the values the tensor core multiplied) -- into
+// per-slot arrays (no atomics, so the results stay bit-reproducible);
+// group_energy_kernel adds the slots in a fixed order and stores each cell's
+// delta = E_exact / E_tensor - 1, and the next step scales that cell's
+// integrals by (1 + delta).  This removes the cell's isotropic bias, the part
+// that a relaxed iteration would otherwise compound step after step.
+//
 // Every mbarrier wait is bounded (rts_ptx::mbar_wait); a wait that gives up
 // sets the device flag, every role stops at its next wait, and the kernel
 // drains and exits.
@@ -93,7 +107,20 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     double* S64;          // [groups][Mout][N], FP64 (host-buffer calls); used instead of S32 when set
     uint16_t* a[2];       // [rows_pad][2*kpad] interleaved split rows
     unsigned long long* resid;  // residual bits of this problem's step
+    // energy-conservation correction of relaxed steps (null: none)
+    const float* vrow;    // [kpad] v_j = sum_k W[j][k], 0 past M
+    double* part;         // [n_tiles * 4][rows_pad][2] per-slot partials: sum_j v_j x_j, sum_k raw_k
+    float* delta;         // [rows_pad] per-cell correction of the next step (0: none yet)
 };
+
+// Kahan-compensated FP32 sum (true sum ~ s - c).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x)
+{
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
 
 __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob, int64_t t)
 {
@@ -113,7 +140,8 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
 // past `nk` become zero (the padding of the split rows).  Returns true when
 // an FP16 value leaves the range the row scale allows.
 template <bool kFp16>
-__device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk)
+__device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk,
+                                       const float* vr, float& es, float& ec)
 {
     const uint4 rh = *hp, rl = *lp;
     const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
@@ -123,6 +151,10 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
         const float2 i2 = rts_ptx::join2_any(kFp16, hw[j >> 1], lw[j >> 1]);
+        if (vr) {  // the split values the tensor core multiplied, weighted by v_j
+            if (j < nk) kahan_add(es, ec, vr[j] * i2.x);
+            if (j + 1 < nk) kahan_add(es, ec, vr[j + 1] * i2.y);
+        }
         const float x0 = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * i2.x) : 0.0f;
         const float x1 = (j + 1 < nk) ? fmaf(snew[j + 1], hrsc, 0.5f * i2.y) : 0.0f;
         if (kFp16) amax = fmaxf(amax, fmaxf(fabsf(x0), fabsf(x1)));
@@ -134,13 +166,15 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
 }
 
 // The same for 4 columns of a split TF32 row (hi and lo as FP32, no scale).
-__device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk)
+__device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk,
+                                            const float* vr, float& es, float& ec)
 {
     const float4 h = *hp, l = *lp;
     const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
     float nh[4], nl[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
+        if (vr && j < nk) kahan_add(es, ec, vr[j] * (hv[j] + lv[j]));
         const float x = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * (hv[j] + lv[j])) : 0.0f;
         rts_ptx::split_tf32(x, nh[j], nl[j]);
     }
@@ -399,7 +433,12 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float lr = lam * ((fp16 && in_row) ? P.rs_inv[r] : 1.0f);
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
-            const float bias = P.bias;
+            const bool want_rel = relax && P.S64 == nullptr;  // relax implies Mout == M <= kpad
+            // energy-conservation correction (relaxed steps): this cell's delta
+            // from the previous step; the partial sums of this one
+            const bool cons = want_rel && P.part != nullptr;
+            const float bias = P.bias + ((cons && in_row) ? P.delta[r] : 0.0f);
+            float ex_s = 0.0f, ex_c = 0.0f, et_s = 0.0f, et_c = 0.0f;
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             const int kbase = n_tile * bn + sw * cs;
@@ -411,7 +450,6 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             // is refilled only once the store that read it has finished reading
             // (rows 4*kpad bytes apart would otherwise cost a line per lane on
             // every access).
-            const bool want_rel = relax && S64 == nullptr;  // relax implies Mout == M <= kpad
             float rmax = 0.0f;
             bool overflow = false;
             // the steps, compiled once per split format (columns per relaxation unit)
@@ -481,7 +519,11 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     tmem_ld8(last_acc + (uint32_t)e0, v);
                     float snew[8];
     #pragma unroll
-                    for (int j = 0; j < 8; ++j) snew[j] = fmaf(fmaf(v[j], bias, v[j]) * cin[j], lr, bterm);
+                    for (int j = 0; j < 8; ++j) {
+                        const float raw = v[j] * cin[j];  // cin is a power of two: exact
+                        if (cons && live_k && j < nk) kahan_add(et_s, et_c, raw);
+                        snew[j] = fmaf(fmaf(raw, bias, raw), lr, bterm);
+                    }
                     if (live_k) {
                         if (S64) {
                             double* dp = S64 + (int64_t)k0 * ld;
@@ -520,16 +562,29 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         uint8_t* rb = rbuf + b * 1024u;
                         const int nku = min(ucols, Mout - (kbase + u * ucols));
                         if (in_row) {
+                            // v_j of the unit's columns (the same for every lane)
+                            float vr[8];
+                            if (cons) {
+                                const float4* vp = reinterpret_cast<const float4*>(P.vrow + kbase + u * ucols);
+                                const float4 v0 = __ldg(vp);
+                                vr[0] = v0.x, vr[1] = v0.y, vr[2] = v0.z, vr[3] = v0.w;
+                                if (!tf32) {
+                                    const float4 v1 = __ldg(vp + 1);
+                                    vr[4] = v1.x, vr[5] = v1.y, vr[6] = v1.z, vr[7] = v1.w;
+                                }
+                            }
+                            const float* vrp = cons ? vr : nullptr;
                             if (tf32) {
                                 relax4_tf32(reinterpret_cast<float4*>(rb + 16 * lane),
-                                            reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku);
+                                            reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku,
+                                            vrp, ex_s, ex_c);
                             } else {
                                 uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
                                 uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
                                 if (fp16)
-                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku);
+                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, ex_s, ex_c);
                                 else
-                                    relax8<false>(hp, lp, snew, hrsc, nku);
+                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, ex_s, ex_c);
                             }
                         }
                         fence_proxy_async_smem();
@@ -553,6 +608,11 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             else
                 run_steps(std::false_type{});
             release_last();
+            if (cons && in_row && ok) {  // this slot's partial sums (coalesced over the warp's 32 rows)
+                const int64_t slot = (int64_t)n_tile * 4 + cs;
+                double2* pp = reinterpret_cast<double2*>(P.part) + slot * (P.m_tiles * (int64_t)G_BM) + r;
+                *pp = make_double2((double)ex_s - (double)ex_c, (double)et_s - (double)et_c);
+            }
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
 #pragma unroll
@@ -568,6 +628,35 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, G_TMEM_COLS);
+    }
+}
+
+// After a relaxed step: each cell's correction for the next step, from the
+// per-slot partial sums of the step (added in a fixed slot order):
+// delta = sum_j v_j I_j / sum_k raw_k - 1, or 0 when either sum is not
+// positive or the ratio is far from 1 (a W with cancelling signs).
+// blockIdx.y: problem; only problems whose step ended in this launch.
+__global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int nprob)
+{
+    const GroupProblem& P = probs[blockIdx.y];
+    if (!(P.relax && P.flip && P.part && P.S64 == nullptr)) return;
+    const int64_t ld = P.m_tiles * (int64_t)G_BM;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        double ex = 0.0, et = 0.0;
+        for (int nt = 0; nt < P.n_tiles; ++nt)
+            for (int cs = 0; cs < 4; ++cs) {
+                if (P.sw * cs >= P.bn) continue;  // a column slice without columns
+                const double2 v = reinterpret_cast<const double2*>(P.part)[((int64_t)nt * 4 + cs) * ld + r];
+                ex += v.x;
+                et += v.y;
+            }
+        float d = 0.0f;
+        if (ex > 0.0 && et > 0.0) {
+            const double g = ex / et - 1.0;
+            if (fabs(g) < 1e-4) d = (float)g;
+        }
+        P.delta[r] = d;
     }
 }
 

@@ -169,7 +169,7 @@ struct rts_ctx {
     cudaEvent_t ev_sync[RTS_STREAM_COUNT] = {};   // rts_sync_stream deadlines
     rts_split_state split;
     int split_flush = 0;         // hi*hi drain period in stages (0: default)
-    int split_bias = 0;          // truncation-bias correction: 0 calibrated, -1 none, >0 custom (1e-10 units)
+    int split_bias = 0;          // truncation correction: 0 conservation-based (relaxed steps), -1 none, >0 constant (1e-10 units)
     int tuning_epoch = 0;        // bumped when a setting that batch tables copy changes
     int64_t w_version = 0;       // bumped whenever d_W is rewritten
     int sweep_cache = 1;         // rts_sweep: store the attenuation factors once per medium (RTS_TUNE_SWEEP_CACHE)
@@ -227,6 +227,8 @@ int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int6
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
+// v[j] = sum_{k < Mout} W[j][k] in FP64, stored as FP32, for j < Min; 0 up to kpad.
+int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st);
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 
 // Tensor-core path (rts_split.cu).

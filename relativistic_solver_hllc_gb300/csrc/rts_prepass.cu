@@ -34,6 +34,19 @@ __device__ __forceinline__ float pow2_scale(double m)
 }
 
 // W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
+// v[j] = sum_k W[j][k] (FP64, k in order), one thread per in-direction j;
+// zero for the padding j >= Min.
+__global__ void row_sums_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad,
+                                float* __restrict__ v)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kpad) return;
+    double s = 0.0;
+    if (j < Min)
+        for (int k = 0; k < Mout; ++k) s += W[(int64_t)j * ldw + k];
+    v[j] = (float)s;
+}
+
 __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad, int mpad,
                                int mode, uint16_t* __restrict__ Wc, float* __restrict__ cs)
 {
@@ -257,6 +270,14 @@ int blocks_for(rts_ctx* ctx, int64_t n, int threads)
 }
 
 }  // namespace
+
+int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st)
+{
+    row_sums_kernel<<<(kpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, v);
+    RTS_CHECK_LAUNCH(ctx, "row_sums_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
 
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
                    uint16_t* Wc, float* cs, cudaStream_t st)

@@ -59,6 +59,8 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
     const float lam = (float)lambda;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(p->lam, &lam, sizeof(float), cudaMemcpyHostToDevice, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
+    rc = rts_group_reset_energy(ctx, p, st);  // the restarted iteration's first step is uncorrected
+    if (rc != RTS_OK) return rc;
     RTS_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // the host lambda must outlive its copy
     rts_group_invalidate(*pb);  // the batch table caches cur / S64 / use_B
     return RTS_OK;
