@@ -63,9 +63,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-serve", action="store_true", help="skip the short serving stream of the default line")
     ap.add_argument("--serve-window", type=float, default=2.0, help="arrival window of that stream, seconds")
-    ap.add_argument("--flush", type=int, default=2, choices=[0, 1, 2],
-                    help="tensor-core K-slices per FP32 drain (library default 1; 2 halves the drains and "
-                         "still meets the 1e-6 gate on this workload, checked in the same run)")
+    ap.add_argument("--flush", type=int, default=0, choices=[0, 1, 2],
+                    help="tensor-core K-slices per FP32 drain (0: the library's automatic choice, which is 2 "
+                         "for this workload's smooth Thomson kernel)")
     ap.add_argument("--moments", action="store_true",
                     help="time the FP64 moment kernels on the config 2 Illum instead (one JSON line)")
     ap.add_argument("--sweep", action="store_true",
@@ -540,6 +540,7 @@ def run_ours(args, rank, world, local):
     ctx.init(xyz, area, fa, N)
     if args.flush:
         ctx.set_tuning(_native.TUNE_FLUSH, args.flush)
+    flush_used = ctx.flush_period()
 
     def fresh(precision):
         ctx.synth_illum(WORKLOAD["seed"], WORKLOAD["mu"], WORKLOAD["sigma"])
@@ -767,7 +768,10 @@ def run_ours(args, rank, world, local):
         "ms_per_step": elapsed / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": dtype, "data": "synthetic",
         "config": {"workload": WORKLOAD["name"], "cells": N, "dirs": M, "precision": prec,
-                   "flush": args.flush or 1,
+                   "flush": flush_used,
+                   "truncation_correction": "relaxed steps: each cell's integrals scaled by the previous step's "
+                                            "ratio sum_j v_j I_j / sum_k S_k (v = W 1, FP64; conserved), no "
+                                            "constant factor; single evaluations uncorrected",
                    "accuracy_gate": "max rel err vs FP64 path <= 1e-6 after the timed steps (see accuracy)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (no flush)", "step": "integral + update + residual + relaxation"},

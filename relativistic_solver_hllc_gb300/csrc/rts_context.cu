@@ -884,6 +884,13 @@ int rts_get_precision(const rts_ctx* ctx, int* precision)
     return RTS_OK;
 }
 
+int rts_flush_period(const rts_ctx* ctx, int* flush)
+{
+    if (!ctx || !flush) return RTS_ERR_INVALID_ARGUMENT;
+    *flush = rts_ctx_flush(ctx);
+    return RTS_OK;
+}
+
 int rts_stream_handle(rts_ctx* ctx, int stream, void** handle)
 {
     if (!ctx || !handle) return RTS_ERR_INVALID_ARGUMENT;

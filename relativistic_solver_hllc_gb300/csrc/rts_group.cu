@@ -108,7 +108,7 @@ void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
     rts_pfree(ctx, p->B, (size_t)(p->rows * 4), st);
     rts_pfree(ctx, p->lam, (size_t)(p->groups * 4), st);
     rts_pfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4), st);
-    rts_pfree(ctx, p->vrow, (size_t)(p->kpad * 4), st);
+    rts_pfree(ctx, p->vrow, (size_t)((p->kpad + 1) * 4), st);
     rts_pfree(ctx, p->part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), st);
     rts_pfree(ctx, p->delta, (size_t)(p->rows_pad * 4), st);
     delete p;
@@ -152,7 +152,7 @@ float rts_group_bias(const rts_ctx* ctx, int, int)
 
 int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles)
 {
-    return kpad * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 4;
+    return (kpad + 1) * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 4;
 }
 
 // Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
@@ -232,7 +232,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
         GP_ALLOC(S32, (size_t)(p->rows * p->Mout * 4), "FP32 scattering");
     }
     if (energy) {
-        GP_ALLOC(vrow, (size_t)(p->kpad * 4), "W row sums");
+        GP_ALLOC(vrow, (size_t)((p->kpad + 1) * 4), "W row sums");
         GP_ALLOC(part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), "energy partial sums");
         GP_ALLOC(delta, (size_t)(p->rows_pad * 4), "energy corrections");
     }
@@ -365,6 +365,7 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.vrow = energy ? p->vrow : nullptr;
     g.part = energy ? p->part : nullptr;
     g.delta = energy ? p->delta : nullptr;
+    g.rsb = p->rs;
     p->slot = (int)i;
     tiles += p->m_tiles * p->n_tiles;
 }

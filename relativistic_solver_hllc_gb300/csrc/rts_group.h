@@ -35,8 +35,8 @@ struct GProb {
     int slot = -1;           // index of the problem's residual in the last launched table
     size_t bytes = 0;
     // energy-conservation correction of relaxed steps (iterative problems)
-    float* vrow = nullptr;   // [kpad] v_j = sum_k W[j][k]
-    double* part = nullptr;  // [n_tiles * 4][rows_pad][2] per-slot partial sums of a step
+    float* vrow = nullptr;   // [kpad + 1] v_j = sum_k W[j][k]; [kpad]: the quantum scale of the partial sums
+    long long* part = nullptr;  // [n_tiles * 4][rows_pad][2] per-slot partial sums of a step (integer quanta)
     float* delta = nullptr;  // [rows_pad] per-row correction of the next step
     alignas(64) unsigned char maps[3][128];
     alignas(64) unsigned char rmaps[2][128];  // relaxation boxes of a[0], a[1]

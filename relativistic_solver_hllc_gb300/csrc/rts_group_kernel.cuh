@@ -44,11 +44,15 @@
 // Every relaxed step writes, per cell and per epilogue warp, the two partial
 // sums -- of the raw integrals it produced and of v_j times the split
 // intensities it read (the values the tensor core multiplied) -- into
-// per-slot arrays (no atomics, so the results stay bit-reproducible);
-// group_energy_kernel adds the slots in a fixed order and stores each cell's
+// per-slot arrays; group_energy_kernel adds the slots and stores each cell's
 // delta = E_exact / E_tensor - 1, and the next step scales that cell's
 // integrals by (1 + delta).  This removes the cell's isotropic bias, the part
-// that a relaxed iteration would otherwise compound step after step.
+// that a relaxed iteration would otherwise compound step after step.  The
+// partial sums are exact integers: each block of 8 columns (4 for TF32) is
+// summed in FP32 in column order and converted to a multiple of a per-row
+// power-of-two quantum (2^-61 of a bound on the row's totals), so neither the
+// order of the additions nor the tiling of the out-directions changes delta,
+// and results stay bit-identical across tile widths and runs.
 //
 // Every mbarrier wait is bounded (rts_ptx::mbar_wait); a wait that gives up
 // sets the device flag, every role stops at its next wait, and the kernel
@@ -108,18 +112,21 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     uint16_t* a[2];       // [rows_pad][2*kpad] interleaved split rows
     unsigned long long* resid;  // residual bits of this problem's step
     // energy-conservation correction of relaxed steps (null: none)
-    const float* vrow;    // [kpad] v_j = sum_k W[j][k], 0 past M
-    double* part;         // [n_tiles * 4][rows_pad][2] per-slot partials: sum_j v_j x_j, sum_k raw_k
+    const float* vrow;    // [kpad + 1] v_j = sum_k W[j][k], 0 past M; vrow[kpad] = q0 (below)
+    long long* part;      // [n_tiles * 4][rows_pad][2] per-slot partials (quanta): sum_j v_j x_j, sum_k raw_k
     float* delta;         // [rows_pad] per-cell correction of the next step (0: none yet)
+    const float* rsb;     // [rows_pad] power of two with rsb * 2 max(|Ibar|, |B|) < 2^14 (all modes)
 };
 
-// Kahan-compensated FP32 sum (true sum ~ s - c).
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x)
+// Quanta per unit of a row's partial sums: q0 * (the row's scale for the
+// unscaled formats), a power of two with q * (bound of the row's totals) <=
+// 2^61.  q0 = 2^(47 - ceil(log2 sum_jk |W_jk|)) comes with vrow; values in
+// the units the epilogue sees are below 2^14 (FP16, scaled) or 2^14 / rsb
+// (BF16, TF32).  0 when out of FP32 range (no correction for the row).
+__device__ __forceinline__ float energy_quantum(const GroupProblem& P, int64_t r, bool fp16)
 {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
+    const float q = P.vrow[P.kpad] * (fp16 ? 1.0f : P.rsb[r]);
+    return (q > 0.0f && q < 3.0e38f) ? q : 0.0f;
 }
 
 __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob, int64_t t)
@@ -141,19 +148,19 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
 // an FP16 value leaves the range the row scale allows.
 template <bool kFp16>
 __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk,
-                                       const float* vr, float& es, float& ec)
+                                       const float* vr, float q, long long& eq)
 {
     const uint4 rh = *hp, rl = *lp;
     const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
     const uint32_t lw[4] = {rl.x, rl.y, rl.z, rl.w};
     uint32_t nh[4], nl[4];
-    float amax = 0.0f;
+    float amax = 0.0f, eb = 0.0f;
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
         const float2 i2 = rts_ptx::join2_any(kFp16, hw[j >> 1], lw[j >> 1]);
         if (vr) {  // the split values the tensor core multiplied, weighted by v_j
-            if (j < nk) kahan_add(es, ec, vr[j] * i2.x);
-            if (j + 1 < nk) kahan_add(es, ec, vr[j + 1] * i2.y);
+            if (j < nk) eb = fmaf(vr[j], i2.x, eb);
+            if (j + 1 < nk) eb = fmaf(vr[j + 1], i2.y, eb);
         }
         const float x0 = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * i2.x) : 0.0f;
         const float x1 = (j + 1 < nk) ? fmaf(snew[j + 1], hrsc, 0.5f * i2.y) : 0.0f;
@@ -162,24 +169,27 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
     }
     *hp = make_uint4(nh[0], nh[1], nh[2], nh[3]);
     *lp = make_uint4(nl[0], nl[1], nl[2], nl[3]);
+    if (vr) eq += __float2ll_rn(eb * q);  // q is a power of two: exact scaling
     return amax > 60000.0f;
 }
 
 // The same for 4 columns of a split TF32 row (hi and lo as FP32, no scale).
 __device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk,
-                                            const float* vr, float& es, float& ec)
+                                            const float* vr, float q, long long& eq)
 {
     const float4 h = *hp, l = *lp;
     const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
     float nh[4], nl[4];
+    float eb = 0.0f;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        if (vr && j < nk) kahan_add(es, ec, vr[j] * (hv[j] + lv[j]));
+        if (vr && j < nk) eb = fmaf(vr[j], hv[j] + lv[j], eb);
         const float x = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * (hv[j] + lv[j])) : 0.0f;
         rts_ptx::split_tf32(x, nh[j], nl[j]);
     }
     *hp = make_float4(nh[0], nh[1], nh[2], nh[3]);
     *lp = make_float4(nl[0], nl[1], nl[2], nl[3]);
+    if (vr) eq += __float2ll_rn(eb * q);
 }
 
 __global__ void __launch_bounds__(G_THREADS, 1)
@@ -436,9 +446,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const bool want_rel = relax && P.S64 == nullptr;  // relax implies Mout == M <= kpad
             // energy-conservation correction (relaxed steps): this cell's delta
             // from the previous step; the partial sums of this one
-            const bool cons = want_rel && P.part != nullptr;
-            const float bias = P.bias + ((cons && in_row) ? P.delta[r] : 0.0f);
-            float ex_s = 0.0f, ex_c = 0.0f, et_s = 0.0f, et_c = 0.0f;
+            const float qrow = (want_rel && P.part != nullptr && in_row) ? energy_quantum(P, r, fp16) : 0.0f;
+            const bool cons = qrow > 0.0f;
+            const float bias = P.bias + (cons ? P.delta[r] : 0.0f);
+            long long ex_q = 0, et_q = 0;  // partial sums in quanta of qrow
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             const int kbase = n_tile * bn + sw * cs;
@@ -518,12 +529,14 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     float v[8];
                     tmem_ld8(last_acc + (uint32_t)e0, v);
                     float snew[8];
+                    float eb = 0.0f;  // this block's raw integrals, in column order
     #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const float raw = v[j] * cin[j];  // cin is a power of two: exact
-                        if (cons && live_k && j < nk) kahan_add(et_s, et_c, raw);
+                        if (j < nk) eb += raw;
                         snew[j] = fmaf(fmaf(raw, bias, raw), lr, bterm);
                     }
+                    if (cons && live_k) et_q += __float2ll_rn(eb * qrow);
                     if (live_k) {
                         if (S64) {
                             double* dp = S64 + (int64_t)k0 * ld;
@@ -577,14 +590,14 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                             if (tf32) {
                                 relax4_tf32(reinterpret_cast<float4*>(rb + 16 * lane),
                                             reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku,
-                                            vrp, ex_s, ex_c);
+                                            vrp, qrow, ex_q);
                             } else {
                                 uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
                                 uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
                                 if (fp16)
-                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, ex_s, ex_c);
+                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, qrow, ex_q);
                                 else
-                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, ex_s, ex_c);
+                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, qrow, ex_q);
                             }
                         }
                         fence_proxy_async_smem();
@@ -608,10 +621,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             else
                 run_steps(std::false_type{});
             release_last();
-            if (cons && in_row && ok) {  // this slot's partial sums (coalesced over the warp's 32 rows)
+            if (want_rel && P.part != nullptr && in_row && ok) {  // this slot's partial sums (zero: no correction)
                 const int64_t slot = (int64_t)n_tile * 4 + cs;
-                double2* pp = reinterpret_cast<double2*>(P.part) + slot * (P.m_tiles * (int64_t)G_BM) + r;
-                *pp = make_double2((double)ex_s - (double)ex_c, (double)et_s - (double)et_c);
+                longlong2* pp = reinterpret_cast<longlong2*>(P.part) + slot * (P.m_tiles * (int64_t)G_BM) + r;
+                *pp = make_longlong2(ex_q, et_q);
             }
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
@@ -643,17 +656,17 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
     const int64_t ld = P.m_tiles * (int64_t)G_BM;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.rows;
          r += (int64_t)gridDim.x * blockDim.x) {
-        double ex = 0.0, et = 0.0;
+        long long ex = 0, et = 0;  // exact: integer quanta
         for (int nt = 0; nt < P.n_tiles; ++nt)
             for (int cs = 0; cs < 4; ++cs) {
                 if (P.sw * cs >= P.bn) continue;  // a column slice without columns
-                const double2 v = reinterpret_cast<const double2*>(P.part)[((int64_t)nt * 4 + cs) * ld + r];
+                const longlong2 v = reinterpret_cast<const longlong2*>(P.part)[((int64_t)nt * 4 + cs) * ld + r];
                 ex += v.x;
                 et += v.y;
             }
         float d = 0.0f;
-        if (ex > 0.0 && et > 0.0) {
-            const double g = ex / et - 1.0;
+        if (ex > 0 && et > 0) {
+            const double g = (double)ex / (double)et - 1.0;
             if (fabs(g) < 1e-4) d = (float)g;
         }
         P.delta[r] = d;

@@ -220,16 +220,31 @@ int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_ar
 inline int rts_split_mode(int precision) { return precision == RTS_PREC_FP16X3 ? 1 : precision == RTS_PREC_TF32X3 ? 2 : 0; }
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
                    uint16_t* Wc, float* cs, cudaStream_t st);
+// rs: per-row power-of-two scales putting 2 max(|Ibar|, |B|) into [2^13, 2^14)
+// (and their inverses), computed in FP16 mode -- where the split applies them --
+// and, with `bound`, in the other modes too, where they only bound the rows.
 int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B, int mode,
-                           float* rs, int64_t npad, uint16_t* A, cudaStream_t st);
+                           float* rs, int64_t npad, uint16_t* A, cudaStream_t st, bool bound = false);
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
-                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st);
+                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st, bool bound = false);
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
-// v[j] = sum_{k < Mout} W[j][k] in FP64, stored as FP32, for j < Min; 0 up to kpad.
+// v[j] = sum_{k < Mout} W[j][k] in FP64, stored as FP32, for j < Min; 0 up to
+// kpad; v[kpad] = 2^(47 - ceil(log2 sum_jk |W_jk|)) (the quantum scale of the
+// relaxed steps' energy partial sums).
 int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st);
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
+
+// Drain period (K-slices per FP32 drain) of the tensor-core path for a
+// direction set, its out-direction columns [k0, k1) and phase kernel: 2 when
+// W is smooth enough that the longer truncation chains stay far below the
+// 1e-6 budget, else 1 (rts_flush.cpp).
+int rts_auto_flush(const double* xyz, const double* area, int64_t M, double full_area, int64_t k0, int64_t k1,
+                   int phase, double g);
+// The context's drain period: RTS_TUNE_FLUSH when set, else rts_auto_flush of
+// its directions, local out-directions and phase kernel.
+int rts_ctx_flush(const rts_ctx* ctx);
 
 // Tensor-core path (rts_split.cu).
 int rts_tuned_bn(const rts_ctx* ctx, int64_t M, int mode, int flush);

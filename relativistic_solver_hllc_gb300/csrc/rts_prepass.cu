@@ -34,17 +34,37 @@ __device__ __forceinline__ float pow2_scale(double m)
 }
 
 // W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
-// v[j] = sum_k W[j][k] (FP64, k in order), one thread per in-direction j;
-// zero for the padding j >= Min.
-__global__ void row_sums_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad,
-                                float* __restrict__ v)
+// v[j] = sum_k W[j][k] (FP64, k in order) for j < Min, 0 up to kpad, and in
+// v[kpad] the quantum scale of the energy partial sums,
+// 2^(47 - ceil(log2 sum_jk |W_jk|)).  One block.
+__global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict__ W, int Min, int Mout, int ldw,
+                                                       int kpad, float* __restrict__ v)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= kpad) return;
-    double s = 0.0;
-    if (j < Min)
-        for (int k = 0; k < Mout; ++k) s += W[(int64_t)j * ldw + k];
-    v[j] = (float)s;
+    __shared__ double tot[32];
+    double a = 0.0;
+    for (int j = threadIdx.x; j < kpad; j += blockDim.x) {
+        double s = 0.0;
+        if (j < Min)
+            for (int k = 0; k < Mout; ++k) {
+                const double w = W[(int64_t)j * ldw + k];
+                s += w;
+                a += fabs(w);
+            }
+        v[j] = (float)s;
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) tot[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tot[w];
+        float q = 0.0f;
+        if (t > 0.0 && isfinite(t)) {
+            const int e = 47 - (int)ceil(log2(t));
+            if (e > -126 && e < 127) q = ldexpf(1.0f, e);
+        }
+        v[kpad] = q;
+    }
 }
 
 __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad, int mpad,
@@ -273,8 +293,8 @@ int blocks_for(rts_ctx* ctx, int64_t n, int threads)
 
 int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st)
 {
-    row_sums_kernel<<<(kpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, v);
-    RTS_CHECK_LAUNCH(ctx, "row_sums_kernel");
+    w_stats_kernel<<<1, 1024, 0, st>>>(W, Min, Mout, ldw, kpad, v);
+    RTS_CHECK_LAUNCH(ctx, "w_stats_kernel");
     ctx->launches++;
     return RTS_OK;
 }
@@ -289,10 +309,10 @@ int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, in
 }
 
 int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad, const double* B,
-                           int mode, float* rs, int64_t npad, uint16_t* A, cudaStream_t st)
+                           int mode, float* rs, int64_t npad, uint16_t* A, cudaStream_t st, bool bound)
 {
     const bool fp16 = mode == 1;
-    if (fp16) {
+    if (fp16 || bound) {  // the scales; the unscaled formats keep them only as a bound of the rows
         rowscale_faces_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(illum, N, ld, M, B, rs, npad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_faces_kernel");
         ctx->launches++;
@@ -305,10 +325,10 @@ int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t
 }
 
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
-                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st)
+                         int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st, bool bound)
 {
     const bool fp16 = mode == 1;
-    if (fp16) {
+    if (fp16 || bound) {
         rowscale_f32_kernel<<<(unsigned)((rows_pad + 127) / 128), 128, 0, st>>>(ibar, N, M, rows, B, rs, rows_pad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_f32_kernel");
         ctx->launches++;

@@ -50,6 +50,12 @@ extern "C" int rts_autotune(rts_ctx* ctx, int64_t M, int precision, int flush, i
                 "rts_autotune: precision %d is not a tensor-core precision", precision);
     RTS_REQUIRE(ctx, flush >= 0 && flush <= 2, RTS_ERR_INVALID_ARGUMENT, "rts_autotune: flush %d outside [0,2]", flush);
     if (cells <= 0) cells = (int64_t)ctx->num_sms * 128 * 4;  // four waves of row tiles
+    if (flush == 0) {  // the automatic drain period of the tuning problem (Thomson, Fibonacci directions)
+        std::vector<double> xyz(3 * (size_t)M), area((size_t)M);
+        double fa = 0.0;
+        rts_synth_directions(M, xyz.data(), area.data(), &fa);
+        flush = rts_auto_flush(xyz.data(), area.data(), M, fa, 0, M, RTS_PHASE_THOMSON, 0.0);
+    }
     RTS_REQUIRE(ctx, cells <= ((int64_t)1 << 26), RTS_ERR_INVALID_ARGUMENT, "rts_autotune: %lld cells",
                 (long long)cells);
 

@@ -1,15 +1,21 @@
-"""The tensor-core source iteration at the setting the benchmark runs: two
-K-slices per FP32 drain (RTS_TUNE_FLUSH 2), with the library's shipped
-truncation-bias correction, on 65,536 cells.
+"""Accuracy of the relaxed tensor-core source iteration on 65,536 cells,
+with the library's correction of the truncating accumulate, at the drain
+periods the library uses.
 
 Every case runs a relaxed source iteration (S = (1 - lambda) B + lambda W^T
 Ibar, Ibar <- 0.5 Ibar + 0.5 S) at fp16x3 or tf32x3 and compares the final S
 of every cell with the FP64 path on the same device inputs, and the S of a
 block of cells with the oracle's FP64 iteration (the restated reference
-integral).  The cases vary what the correction could depend on: the spread
-of the intensities (lognormal sigma 0.5 to 2), the direction count (146 to
+integral).  The cases vary what the accuracy could depend on: the spread of
+the intensities (lognormal sigma 0.5 to 2), the direction count (146 to
 1202), the phase kernel (Thomson, Henyey-Greenstein g = 0.8), the albedo and
 the number of relaxed steps (20, and 40 as the longest serving requests).
+
+* test_default_setting: every case at the library's default drain period
+  (automatic: two K-slices per drain only for smooth kernels);
+* test_two_slices_per_drain_on_smooth_kernels: the benchmark's setting --
+  two K-slices per drain forced -- on the Thomson cases, the ones the
+  automatic choice gives it to.
 
 Tolerance: max relative error <= 1e-6 after the last step (the accuracy gate
 of the tensor path), for the max over all cells and for the oracle block.
@@ -40,6 +46,7 @@ CASES = [
     (1.0, 1000, PHASE_THOMSON, 0.0, 0.95, 40),
     (1.0, 302, PHASE_HG, 0.8, 0.9, 40),
 ]
+SMOOTH = [c for c in CASES if c[2] == PHASE_THOMSON and c[1] >= 302]
 
 
 def _case_id(c):
@@ -55,17 +62,16 @@ def _run(ctx, prec, B, lam, steps):
     return ctx.solve_read()
 
 
-@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
-@pytest.mark.parametrize("case", CASES, ids=_case_id)
-def test_relaxed_iteration_flush2(ctx, prec, case):
+def _check(ctx, prec, case, flush):
     sigma, M, phase, g, lam, steps = case
     xyz, area, fa = oracle.fibonacci_directions(M)
     B = oracle.uniform(SEED, 2, 0.1, 1.0, N)
     ctx.init(xyz, area, fa, N)
     if phase == PHASE_HG:
         ctx.set_phase(PHASE_HG, g)
-    ctx.set_tuning(TUNE_FLUSH, 2)
+    ctx.set_tuning(TUNE_FLUSH, flush)
     try:
+        used = ctx.flush_period()
         ctx.synth_illum(SEED, 0.0, sigma)
         S_t = _run(ctx, prec, B, lam, steps)
         ctx.synth_illum(SEED, 0.0, sigma)
@@ -73,7 +79,7 @@ def test_relaxed_iteration_flush2(ctx, prec, case):
     finally:
         ctx.set_tuning(TUNE_FLUSH, 0)
     rel = np.abs(S_t - S_64) / np.abs(S_64)
-    assert float(rel.max()) <= TOL, (float(rel.max()), float(rel.mean()))
+    assert float(rel.max()) <= TOL, (used, float(rel.max()), float(rel.mean()))
 
     # a block of 48 cells against the oracle's FP64 iteration of the same inputs
     c0, c1 = N // 3, N // 3 + 48
@@ -87,3 +93,18 @@ def test_relaxed_iteration_flush2(ctx, prec, case):
     # the FP64 path itself follows the oracle (its own gate is 1e-12 on one
     # evaluation; the iteration compounds a few ulps)
     assert float(np.max(np.abs(S_64[:, c0:c1] - S_ref) / S_ref)) <= 1e-11
+    return used
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
+@pytest.mark.parametrize("case", CASES, ids=_case_id)
+def test_default_setting(ctx, prec, case):
+    used = _check(ctx, prec, case, 0)
+    # the automatic drain period: two K-slices only for the smooth kernels
+    assert used == (2 if case in SMOOTH else 1)
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
+@pytest.mark.parametrize("case", SMOOTH, ids=_case_id)
+def test_two_slices_per_drain_on_smooth_kernels(ctx, prec, case):
+    assert _check(ctx, prec, case, 2) == 2
