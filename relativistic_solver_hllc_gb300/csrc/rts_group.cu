@@ -84,6 +84,7 @@ struct rts_batch {
     size_t staging_bytes = 0;
     double* d_dirs = nullptr;  // xyz + area scratch
     size_t dirs_cap = 0;
+    bool table_energy = false;  // a problem of the device table keeps the energy partial sums
     cudaGraphExec_t gexec = nullptr;
     int graph_steps = 0, graph_relax = 0;
     int64_t total_tiles = 0;
@@ -363,7 +364,7 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     // RTS_TUNE_BIAS -1 switches the conservation-based correction off
     const bool energy = p->part != nullptr && ctx->split_bias >= 0;
     g.vrow = energy ? p->vrow : nullptr;
-    g.part = energy ? p->part : nullptr;
+    g.part = energy ? reinterpret_cast<int4*>(p->part) : nullptr;
     g.delta = energy ? p->delta : nullptr;
     g.rsb = p->rs;
     p->slot = (int)i;
@@ -403,7 +404,11 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
     if (rc != RTS_OK) return rc;
     b->h_table.assign(n, GroupProblem());
     int64_t tiles = 0;
-    for (size_t i = 0; i < n; ++i) fill_entry(b, b->probs[i], relax, i, tiles, b->h_table[i]);
+    b->table_energy = false;
+    for (size_t i = 0; i < n; ++i) {
+        fill_entry(b, b->probs[i], relax, i, tiles, b->h_table[i]);
+        b->table_energy |= b->h_table[i].part != nullptr;
+    }
     b->total_tiles = tiles;
     if (n) RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_table.data(), n * sizeof(GroupProblem),
                                              cudaMemcpyHostToDevice, st));
@@ -415,11 +420,20 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
     return RTS_OK;
 }
 
+// Dynamic shared memory of both instantiations of the kernel.
+static cudaError_t set_kernel_smem()
+{
+    cudaError_t e = cudaFuncSetAttribute(group_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(group_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+    return e;
+}
+
 int rts_group_prepare(rts_batch* b, int relax, cudaStream_t st)
 {
     rts_ctx* ctx = b->ctx;
     if (b->probs.empty()) return RTS_OK;
-    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    RTS_CUDA_TRY(ctx, set_kernel_smem());
     return upload_table(b, relax, st);
 }
 
@@ -430,7 +444,11 @@ static int enqueue_step(rts_batch* b, int relax, cudaStream_t st, int n)
     const int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * G_CTAS_PER_SM, b->total_tiles);
     if (grid > 0) {
         rts_timing_begin(ctx, st);
-        group_kernel<<<(unsigned)grid, G_THREADS, G_SMEM, st>>>(b->d_table, n, b->total_tiles, ctx->d_flag);
+        // the energy bookkeeping is compiled in only where a relaxed problem of the launch uses it
+        if (relax && b->table_energy)
+            group_kernel<true><<<(unsigned)grid, G_THREADS, G_SMEM, st>>>(b->d_table, n, b->total_tiles, ctx->d_flag);
+        else
+            group_kernel<false><<<(unsigned)grid, G_THREADS, G_SMEM, st>>>(b->d_table, n, b->total_tiles, ctx->d_flag);
         rts_timing_end(ctx, st);
         RTS_CHECK_LAUNCH(ctx, "group_kernel");
         ctx->launches++;
@@ -467,7 +485,7 @@ int rts_group_step(rts_batch* b, int relax, cudaStream_t st)
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED,
                 "the tensor-core path needs a Blackwell (sm_10x) device, found sm_%d%d", ctx->cc_major, ctx->cc_minor);
     if (b->probs.empty()) return RTS_OK;
-    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    RTS_CUDA_TRY(ctx, set_kernel_smem());
     int rc = upload_table(b, relax, st);
     if (rc != RTS_OK) return rc;
     rc = enqueue_step(b, relax, st, (int)b->probs.size());
@@ -498,7 +516,7 @@ int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int
         RTS_REQUIRE(ctx, f >= 0 && c > 0 && f + c <= tiles, RTS_ERR_INVALID_ARGUMENT,
                     "tiles [%lld,%lld) outside the problem's %lld", (long long)f, (long long)(f + c), (long long)tiles);
     }
-    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    RTS_CUDA_TRY(ctx, set_kernel_smem());
     int rc = ensure_table(b, (size_t)n, st);
     if (rc != RTS_OK) return rc;
     if (b->pin_cap < (size_t)n) {
@@ -519,10 +537,12 @@ int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int
     b->pin_next ^= 1;
     RTS_CUDA_TRY(ctx, cudaEventSynchronize(b->pin_ev[k]));  // its previous copy has been consumed
     int64_t total = 0;
+    b->table_energy = false;
     for (int i = 0; i < n; ++i) {
         GroupProblem& g = b->h_pin[k][i];
         int64_t ignored = 0;
         fill_entry(b, sel[i], relax, (size_t)i, ignored, g);
+        b->table_energy |= g.part != nullptr;
         const int64_t tiles = sel[i]->m_tiles * sel[i]->n_tiles;
         const int64_t f = first ? first[i] : 0, c = count ? count[i] : tiles;
         g.tile_begin = total;
@@ -564,7 +584,7 @@ int rts_group_capture(rts_batch* b, int steps, int relax)
     RTS_REQUIRE(ctx, !b->probs.empty(), RTS_ERR_BAD_STATE, "capture of an empty batch");
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell device");
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
-    RTS_CUDA_TRY(ctx, cudaFuncSetAttribute(group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM));
+    RTS_CUDA_TRY(ctx, set_kernel_smem());
     int rc = upload_table(b, relax, st);
     if (rc != RTS_OK) return rc;
     drop_graph(b);

@@ -36,7 +36,7 @@ struct GProb {
     size_t bytes = 0;
     // energy-conservation correction of relaxed steps (iterative problems)
     float* vrow = nullptr;   // [kpad + 1] v_j = sum_k W[j][k]; [kpad]: the quantum scale of the partial sums
-    long long* part = nullptr;  // [n_tiles * 4][rows_pad][2] per-slot partial sums of a step (integer quanta)
+    void* part = nullptr;    // [n_tiles * 4][rows_pad] int4 per-slot partial sums of a step (fixed point)
     float* delta = nullptr;  // [rows_pad] per-row correction of the next step
     alignas(64) unsigned char maps[3][128];
     alignas(64) unsigned char rmaps[2][128];  // relaxation boxes of a[0], a[1]

@@ -48,11 +48,13 @@
 // delta = E_exact / E_tensor - 1, and the next step scales that cell's
 // integrals by (1 + delta).  This removes the cell's isotropic bias, the part
 // that a relaxed iteration would otherwise compound step after step.  The
-// partial sums are exact integers: each block of 8 columns (4 for TF32) is
-// summed in FP32 in column order and converted to a multiple of a per-row
-// power-of-two quantum (2^-61 of a bound on the row's totals), so neither the
+// partial sums are exact fixed-point numbers: each block of 8 columns is
+// summed in FP32 in column order and rounded to a multiple of a per-row
+// power-of-two quantum (2^-43 of a bound on the row's totals), so neither the
 // order of the additions nor the tiling of the out-directions changes delta,
-// and results stay bit-identical across tile widths and runs.
+// and results stay bit-identical across tile widths and runs.  The kernel is
+// compiled with and without this bookkeeping (kEnergy); launches without a
+// relaxed problem that uses it run the lighter instantiation.
 //
 // Every mbarrier wait is bounded (rts_ptx::mbar_wait); a wait that gives up
 // sets the device flag, every role stops at its next wait, and the kernel
@@ -70,6 +72,8 @@ constexpr int G_EPI_WARPS = 16;
 constexpr int G_EPI_WARP0 = 3;
 constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
 constexpr int G_CTAS_PER_SM = 1;
+// registers per thread: 19 warps x 32 x 104 = 63,232 of the SM's 65,536
+constexpr int G_MAXREG = 104;
 constexpr uint32_t G_TMEM_COLS = 512;
 constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
 // relaxation row buffers per epilogue warp: G_REL_NB - 1 units are fetched
@@ -113,20 +117,36 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     unsigned long long* resid;  // residual bits of this problem's step
     // energy-conservation correction of relaxed steps (null: none)
     const float* vrow;    // [kpad + 1] v_j = sum_k W[j][k], 0 past M; vrow[kpad] = q0 (below)
-    long long* part;      // [n_tiles * 4][rows_pad][2] per-slot partials (quanta): sum_j v_j x_j, sum_k raw_k
+    int4* part;           // [n_tiles * 4][rows_pad] per-slot partials in quanta (high, low parts):
+                          // sum_j v_j x_j, then sum_k raw_k
     float* delta;         // [rows_pad] per-cell correction of the next step (0: none yet)
     const float* rsb;     // [rows_pad] power of two with rsb * 2 max(|Ibar|, |B|) < 2^14 (all modes)
 };
 
-// Quanta per unit of a row's partial sums: q0 * (the row's scale for the
-// unscaled formats), a power of two with q * (bound of the row's totals) <=
-// 2^61.  q0 = 2^(47 - ceil(log2 sum_jk |W_jk|)) comes with vrow; values in
-// the units the epilogue sees are below 2^14 (FP16, scaled) or 2^14 / rsb
-// (BF16, TF32).  0 when out of FP32 range (no correction for the row).
-__device__ __forceinline__ float energy_quantum(const GroupProblem& P, int64_t r, bool fp16)
+// Scale of a row's partial sums: q0 * (the row's scale for the unscaled
+// formats), a power of two with (scale * bound of the row's totals) <= 2^21.
+// q0 = 2^(7 - ceil(log2 sum_jk |W_jk|)) comes with vrow; values in the units
+// the epilogue sees are below 2^14 (FP16, scaled) or 2^14 / rsb (BF16,
+// TF32).  0 when out of FP32 range (no correction for the row).
+__device__ __forceinline__ float energy_scale(const GroupProblem& P, int64_t r, bool fp16)
 {
     const float q = P.vrow[P.kpad] * (fp16 ? 1.0f : P.rsb[r]);
     return (q > 0.0f && q < 3.0e38f) ? q : 0.0f;
+}
+
+// Adds y (|y| <= 2^21) to an exact fixed-point sum kept as integer high and
+// low parts, hi + lo * 2^-22 (units of 1 and 2^-22): adding 1.5 * 2^23 rounds
+// to an integer in FP32, and the remainder, scaled by 2^22 (exact), is
+// rounded the same way.  No conversion instructions; the sum of such parts is
+// exact in any order.
+__device__ __forceinline__ void fixed_add(float y, int& hi, int& lo)
+{
+    constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
+    const float t = y + MAGIC;
+    const float r = y - (t - MAGIC);
+    const float t2 = fmaf(r, 4194304.0f, MAGIC);
+    hi += __float_as_int(t) - __float_as_int(MAGIC);
+    lo += __float_as_int(t2) - __float_as_int(MAGIC);
 }
 
 __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob, int64_t t)
@@ -148,13 +168,13 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
 // an FP16 value leaves the range the row scale allows.
 template <bool kFp16>
 __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk,
-                                       const float* vr, float q, long long& eq)
+                                       const float* vr, float& eb)
 {
     const uint4 rh = *hp, rl = *lp;
     const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
     const uint32_t lw[4] = {rl.x, rl.y, rl.z, rl.w};
     uint32_t nh[4], nl[4];
-    float amax = 0.0f, eb = 0.0f;
+    float amax = 0.0f;
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
         const float2 i2 = rts_ptx::join2_any(kFp16, hw[j >> 1], lw[j >> 1]);
@@ -169,18 +189,16 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
     }
     *hp = make_uint4(nh[0], nh[1], nh[2], nh[3]);
     *lp = make_uint4(nl[0], nl[1], nl[2], nl[3]);
-    if (vr) eq += __float2ll_rn(eb * q);  // q is a power of two: exact scaling
     return amax > 60000.0f;
 }
 
 // The same for 4 columns of a split TF32 row (hi and lo as FP32, no scale).
 __device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk,
-                                            const float* vr, float q, long long& eq)
+                                            const float* vr, float& eb)
 {
     const float4 h = *hp, l = *lp;
     const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
     float nh[4], nl[4];
-    float eb = 0.0f;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (vr && j < nk) eb = fmaf(vr[j], hv[j] + lv[j], eb);
@@ -189,10 +207,10 @@ __device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float*
     }
     *hp = make_float4(nh[0], nh[1], nh[2], nh[3]);
     *lp = make_float4(nl[0], nl[1], nl[2], nl[3]);
-    if (vr) eq += __float2ll_rn(eb * q);
 }
 
-__global__ void __launch_bounds__(G_THREADS, 1)
+template <bool kEnergy>
+__global__ void __maxnreg__(G_MAXREG)
 group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_tiles, int* flag)
 {
     using namespace rts_ptx;
@@ -445,14 +463,25 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
             const bool want_rel = relax && P.S64 == nullptr;  // relax implies Mout == M <= kpad
             // energy-conservation correction (relaxed steps): this cell's delta
-            // from the previous step; the partial sums of this one
-            const float qrow = (want_rel && P.part != nullptr && in_row) ? energy_quantum(P, r, fp16) : 0.0f;
+            // from the previous step; the partial sums of this one.  `ewarp`
+            // is uniform over the warp (the shuffles of v_j need every lane).
+            const bool ewarp = kEnergy && want_rel && P.part != nullptr;
+            const float qrow = (ewarp && in_row) ? energy_scale(P, r, fp16) : 0.0f;
             const bool cons = qrow > 0.0f;
             const float bias = P.bias + (cons ? P.delta[r] : 0.0f);
-            long long ex_q = 0, et_q = 0;  // partial sums in quanta of qrow
+            int xh = 0, xl = 0, th = 0, tl = 0;  // fixed-point partial sums (sum_j v_j x_j, sum_k raw_k)
+            float vp0 = 0.0f, vp1 = 0.0f;        // v_j of this warp's columns kbase + 2 lane, + 1
+            const int kbase = n_tile * bn + sw * cs;
+            if (ewarp) {
+                const int c0 = kbase + 2 * lane;
+                if (2 * lane < ncols && c0 < P.kpad) {
+                    const float2 v2 = __ldg(reinterpret_cast<const float2*>(P.vrow + c0));
+                    vp0 = v2.x;
+                    vp1 = v2.y;
+                }
+            }
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
-            const int kbase = n_tile * bn + sw * cs;
             // The relaxation's split rows move by TMA in units of 16 B hi and
             // 16 B lo of each of the warp's 32 rows (8 columns of a 16-bit
             // split, 4 of a TF32 split): a 2-D box load into one of two
@@ -529,14 +558,15 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     float v[8];
                     tmem_ld8(last_acc + (uint32_t)e0, v);
                     float snew[8];
-                    float eb = 0.0f;  // this block's raw integrals, in column order
+                    float eb = 0.0f;  // these 8 columns' raw integrals, in column order
     #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const float raw = v[j] * cin[j];  // cin is a power of two: exact
-                        if (j < nk) eb += raw;
+                        if (kEnergy && j < nk) eb += raw;
                         snew[j] = fmaf(fmaf(raw, bias, raw), lr, bterm);
                     }
-                    if (cons && live_k) et_q += __float2ll_rn(eb * qrow);
+                    // blocks of 8 columns start at multiples of 8 of the out-directions
+                    if (kEnergy && cons && live_k) fixed_add(eb * qrow, th, tl);
                     if (live_k) {
                         if (S64) {
                             double* dp = S64 + (int64_t)k0 * ld;
@@ -561,6 +591,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     // place (rows outside the problem stay unchanged), store the box
                     // into the other ping-pong buffer
                     bool stop = false;
+                    float xe = 0.0f;  // sum_j v_j x_j of these 8 columns
                     for (int ui = 0; ui < 8 / ucols; ++ui) {
                         const int u = e0 / ucols + ui;
                         if (u >= u_real) break;
@@ -574,30 +605,26 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         }
                         uint8_t* rb = rbuf + b * 1024u;
                         const int nku = min(ucols, Mout - (kbase + u * ucols));
+                        // v_j of the unit's columns, from the lanes holding them (all lanes shuffle)
+                        float vr[ucols];
+                        if (kEnergy && ewarp) {
+    #pragma unroll
+                            for (int j = 0; j < ucols; ++j)
+                                vr[j] = __shfl_sync(0xffffffffu, (j & 1) ? vp1 : vp0, (u * ucols + j) >> 1);
+                        }
                         if (in_row) {
-                            // v_j of the unit's columns (the same for every lane)
-                            float vr[8];
-                            if (cons) {
-                                const float4* vp = reinterpret_cast<const float4*>(P.vrow + kbase + u * ucols);
-                                const float4 v0 = __ldg(vp);
-                                vr[0] = v0.x, vr[1] = v0.y, vr[2] = v0.z, vr[3] = v0.w;
-                                if (!tf32) {
-                                    const float4 v1 = __ldg(vp + 1);
-                                    vr[4] = v1.x, vr[5] = v1.y, vr[6] = v1.z, vr[7] = v1.w;
-                                }
-                            }
-                            const float* vrp = cons ? vr : nullptr;
+                            const float* vrp = (kEnergy && cons) ? vr : nullptr;
                             if (tf32) {
                                 relax4_tf32(reinterpret_cast<float4*>(rb + 16 * lane),
                                             reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku,
-                                            vrp, qrow, ex_q);
+                                            vrp, xe);
                             } else {
                                 uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
                                 uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
                                 if (fp16)
-                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, qrow, ex_q);
+                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, xe);
                                 else
-                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, qrow, ex_q);
+                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, xe);
                             }
                         }
                         fence_proxy_async_smem();
@@ -614,6 +641,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         ok = false;
                         break;
                     }
+                    if (kEnergy && cons) fixed_add(xe * qrow, xh, xl);  // the same 8-column blocks
                 }
             };
             if (P.tf32)
@@ -621,10 +649,9 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             else
                 run_steps(std::false_type{});
             release_last();
-            if (want_rel && P.part != nullptr && in_row && ok) {  // this slot's partial sums (zero: no correction)
+            if (kEnergy && ewarp && in_row && ok) {  // this slot's partial sums (zero: no correction)
                 const int64_t slot = (int64_t)n_tile * 4 + cs;
-                longlong2* pp = reinterpret_cast<longlong2*>(P.part) + slot * (P.m_tiles * (int64_t)G_BM) + r;
-                *pp = make_longlong2(ex_q, et_q);
+                P.part[slot * (P.m_tiles * (int64_t)G_BM) + r] = make_int4(xh, xl, th, tl);
             }
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
@@ -656,13 +683,13 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
     const int64_t ld = P.m_tiles * (int64_t)G_BM;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.rows;
          r += (int64_t)gridDim.x * blockDim.x) {
-        long long ex = 0, et = 0;  // exact: integer quanta
+        long long ex = 0, et = 0;  // exact: in units of 2^-22 of the row's scale
         for (int nt = 0; nt < P.n_tiles; ++nt)
             for (int cs = 0; cs < 4; ++cs) {
                 if (P.sw * cs >= P.bn) continue;  // a column slice without columns
-                const longlong2 v = reinterpret_cast<const longlong2*>(P.part)[((int64_t)nt * 4 + cs) * ld + r];
-                ex += v.x;
-                et += v.y;
+                const int4 v = P.part[((int64_t)nt * 4 + cs) * ld + r];
+                ex += ((long long)v.x << 22) + v.y;
+                et += ((long long)v.z << 22) + v.w;
             }
         float d = 0.0f;
         if (ex > 0 && et > 0) {

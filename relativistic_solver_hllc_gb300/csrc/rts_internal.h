@@ -231,8 +231,8 @@ int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t 
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
 // v[j] = sum_{k < Mout} W[j][k] in FP64, stored as FP32, for j < Min; 0 up to
-// kpad; v[kpad] = 2^(47 - ceil(log2 sum_jk |W_jk|)) (the quantum scale of the
-// relaxed steps' energy partial sums).
+// kpad; v[kpad] = 2^(7 - ceil(log2 sum_jk |W_jk|)) (the scale of the relaxed
+// steps' energy partial sums).
 int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st);
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 

@@ -35,8 +35,8 @@ __device__ __forceinline__ float pow2_scale(double m)
 
 // W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
 // v[j] = sum_k W[j][k] (FP64, k in order) for j < Min, 0 up to kpad, and in
-// v[kpad] the quantum scale of the energy partial sums,
-// 2^(47 - ceil(log2 sum_jk |W_jk|)).  One block.
+// v[kpad] the scale of the energy partial sums, 2^(7 - ceil(log2 sum_jk
+// |W_jk|)).  One block.
 __global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict__ W, int Min, int Mout, int ldw,
                                                        int kpad, float* __restrict__ v)
 {
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict_
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tot[w];
         float q = 0.0f;
         if (t > 0.0 && isfinite(t)) {
-            const int e = 47 - (int)ceil(log2(t));
+            const int e = 7 - (int)ceil(log2(t));
             if (e > -126 && e < 127) q = ldexpf(1.0f, e);
         }
         v[kpad] = q;
