@@ -409,6 +409,8 @@ static int upload_table(rts_batch* b, int relax, cudaStream_t st)
         fill_entry(b, b->probs[i], relax, i, tiles, b->h_table[i]);
         b->table_energy |= b->h_table[i].part != nullptr;
     }
+    // the energy instantiation runs relaxed iterations only (no FP64 outputs)
+    for (size_t i = 0; i < n; ++i) b->table_energy &= b->h_table[i].S64 == nullptr;
     b->total_tiles = tiles;
     if (n) RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_table.data(), n * sizeof(GroupProblem),
                                              cudaMemcpyHostToDevice, st));
@@ -454,12 +456,15 @@ static int enqueue_step(rts_batch* b, int relax, cudaStream_t st, int n)
         ctx->launches++;
     }
     if (relax) {
-        // each cell's correction of the next step (problems without the
-        // buffers return at once), then the buffer flip
-        const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * ctx->num_sms, 1 << 12));
-        group_energy_kernel<<<dim3(gx, (unsigned)n), 256, 0, st>>>(b->d_table, n);
-        RTS_CHECK_LAUNCH(ctx, "group_energy_kernel");
-        ctx->launches++;
+        // each cell's correction of the next step, after a launch that kept
+        // the partial sums (problems without the buffers return at once);
+        // then the buffer flip
+        if (b->table_energy) {
+            const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * ctx->num_sms, 1 << 12));
+            group_energy_kernel<<<dim3(gx, (unsigned)n), 256, 0, st>>>(b->d_table, n);
+            RTS_CHECK_LAUNCH(ctx, "group_energy_kernel");
+            ctx->launches++;
+        }
         group_flip_kernel<<<(n + 127) / 128, 128, 0, st>>>(b->d_table, n);
         RTS_CHECK_LAUNCH(ctx, "group_flip_kernel");
         ctx->launches++;
@@ -538,11 +543,13 @@ int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int
     RTS_CUDA_TRY(ctx, cudaEventSynchronize(b->pin_ev[k]));  // its previous copy has been consumed
     int64_t total = 0;
     b->table_energy = false;
+    bool energy_blocked = false;
     for (int i = 0; i < n; ++i) {
         GroupProblem& g = b->h_pin[k][i];
         int64_t ignored = 0;
         fill_entry(b, sel[i], relax, (size_t)i, ignored, g);
         b->table_energy |= g.part != nullptr;
+        if (g.S64) energy_blocked = true;
         const int64_t tiles = sel[i]->m_tiles * sel[i]->n_tiles;
         const int64_t f = first ? first[i] : 0, c = count ? count[i] : tiles;
         g.tile_begin = total;
@@ -550,6 +557,7 @@ int rts_group_step_pieces(rts_batch* b, int relax, const int64_t* ids, const int
         g.flip = (g.relax && f + c == tiles) ? 1 : 0;
         total += c;
     }
+    if (energy_blocked) b->table_energy = false;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_table, b->h_pin[k], (size_t)n * sizeof(GroupProblem),
                                       cudaMemcpyHostToDevice, st));
     RTS_CUDA_TRY(ctx, cudaEventRecord(b->pin_ev[k], st));

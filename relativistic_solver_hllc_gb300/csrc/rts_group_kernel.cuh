@@ -72,8 +72,6 @@ constexpr int G_EPI_WARPS = 16;
 constexpr int G_EPI_WARP0 = 3;
 constexpr int G_THREADS = (G_EPI_WARP0 + G_EPI_WARPS) * 32;
 constexpr int G_CTAS_PER_SM = 1;
-// registers per thread: 19 warps x 32 x 104 = 63,232 of the SM's 65,536
-constexpr int G_MAXREG = 104;
 constexpr uint32_t G_TMEM_COLS = 512;
 constexpr int G_MAX_FLUSH = 2;  // K-slices per chunk
 // relaxation row buffers per epilogue warp: G_REL_NB - 1 units are fetched
@@ -210,7 +208,7 @@ __device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float*
 }
 
 template <bool kEnergy>
-__global__ void __maxnreg__(G_MAXREG)
+__global__ void __launch_bounds__(G_THREADS, 1)
 group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_tiles, int* flag)
 {
     using namespace rts_ptx;
@@ -461,7 +459,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float lr = lam * ((fp16 && in_row) ? P.rs_inv[r] : 1.0f);
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
-            const bool want_rel = relax && P.S64 == nullptr;  // relax implies Mout == M <= kpad
+            const bool want_rel = relax && (kEnergy || P.S64 == nullptr);  // relax implies Mout == M <= kpad
             // energy-conservation correction (relaxed steps): this cell's delta
             // from the previous step; the partial sums of this one.  `ewarp`
             // is uniform over the warp (the shuffles of v_j need every lane).
@@ -481,7 +479,8 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                 }
             }
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
-            double* __restrict__ S64 = P.S64 ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
+            // (the energy instantiation runs relaxed source iterations, whose output is S32)
+            double* __restrict__ S64 = (!kEnergy && P.S64) ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
             // The relaxation's split rows move by TMA in units of 16 B hi and
             // 16 B lo of each of the warp's 32 rows (8 columns of a 16-bit
             // split, 4 of a TF32 split): a 2-D box load into one of two
