@@ -540,7 +540,7 @@ def run_ours(args, rank, world, local):
     ctx.init(xyz, area, fa, N)
     if args.flush:
         ctx.set_tuning(_native.TUNE_FLUSH, args.flush)
-    flush_used = ctx.flush_period()
+    flush_used = ctx.flush_period(prec) if prec != "fp64" else None
 
     def fresh(precision):
         ctx.synth_illum(WORKLOAD["seed"], WORKLOAD["mu"], WORKLOAD["sigma"])
@@ -702,6 +702,8 @@ def run_ours(args, rank, world, local):
                  "p50_ms": row["p50_ms"], "p99_ms": row["p99_ms"],
                  "isolated_p50_ms": row.get("isolated_p50_ms"), "isolated_p99_ms": row.get("isolated_p99_ms"),
                  "p99_over_isolated_p99": row.get("p99_vs_isolated_p99"),
+                 "fifo_alone_p99_ms": row.get("fifo_alone_p99_ms"),
+                 "fifo_alone_p99_over_isolated_p99": row.get("fifo_alone_p99_vs_isolated_p99"),
                  "mean_queue_ms": row.get("mean_queue_ms"), "p99_queue_ms": row.get("p99_queue_ms"),
                  "throughput_cell_dir_iter_per_s": row["throughput_cell_dir_iter_per_s"],
                  "policy": sres["policy"], "window_s": args.serve_window,

@@ -320,7 +320,7 @@ typedef struct rts_problem_desc {
     int phase;      /* RTS_PHASE_THOMSON or RTS_PHASE_HG */
     double g;       /* Henyey-Greenstein asymmetry, (-1, 1) */
     int precision;  /* RTS_PREC_FP16X3 or RTS_PREC_BF16X3 */
-    int flush;      /* K-slices per FP32 drain (1 or 2; 0: automatic, 2 only for smooth kernels, see RTS_TUNE_FLUSH) */
+    int flush;      /* K-slices per FP32 drain (1 or 2; 0: automatic, see RTS_TUNE_FLUSH) */
     int bn;         /* out-directions per tile, multiple of 16, <= 256 (0: balanced default) */
 } rts_problem_desc;
 
@@ -579,11 +579,12 @@ int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, 
 /* Tuning knobs of the tensor-core path (0 restores the default):
  *   RTS_TUNE_FLUSH: K-slices (32 in-directions for FP16 / BF16, 16 for TF32)
  *   accumulated on the tensor core before the partial sum is added in FP32
- *   on the CUDA cores: 1 or 2.  The default (0) is automatic: 2 -- half as
- *   many drains -- only when no 16-direction block of any out-direction's
- *   column of W carries more than 1/8 of it (smooth kernels on enough
- *   directions: Thomson at M >= 302, Henyey-Greenstein with small g),
- *   else 1; caller-supplied W uses 1.
+ *   on the CUDA cores: 1 or 2.  The default (0) is automatic: for FP16 and
+ *   BF16, 2 -- half as many drains -- only when no 16-direction block of any
+ *   out-direction's column of W carries more than 1/8 of it (smooth kernels
+ *   on enough directions: Thomson at M >= 302, Henyey-Greenstein with small
+ *   g), else 1 (caller-supplied W: 1); for TF32 always 2 (32 in-directions
+ *   per drain).
  *   RTS_TUNE_BIAS: correction of the tensor core's truncating FP32
  *   accumulation (each accumulate rounds toward zero, so sums come out low by
  *   ~1e-7 of themselves).  0 (default): relaxed source iterations scale each
@@ -592,7 +593,8 @@ int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, 
  *   the integrals is conserved), which removes the part of the loss that
  *   would compound; single evaluations keep the loss of one pass.  -1: no
  *   correction.  n > 0: the default plus a constant factor (1 + n * 1e-10)
- *   on every sum. */
+ *   on every sum.  Takes effect for iterations set up (rts_solve_setup,
+ *   rts_batch_add) after the change. */
 #define RTS_TUNE_FLUSH 1
 #define RTS_TUNE_BIAS 2
 /*   RTS_TUNE_SERVE_POLICY: how rts_serve_run chooses the requests a step
@@ -619,9 +621,9 @@ int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, 
 int rts_set_tuning(rts_ctx* ctx, int key, int value);
 
 /* The drain period (K-slices per FP32 drain) that the context's tensor-core
- * calls use for its current directions, out-directions and phase kernel:
- * RTS_TUNE_FLUSH when set, else the automatic choice. */
-int rts_flush_period(const rts_ctx* ctx, int* flush);
+ * calls at `precision` use for its current directions, out-directions and
+ * phase kernel: RTS_TUNE_FLUSH when set, else the automatic choice. */
+int rts_flush_period(const rts_ctx* ctx, int precision, int* flush);
 
 /* Autotuner of the tensor-core kernel's tile width (out-directions per
  * tile).  Times every distinct tiling of M directions (tiles of 64..256) on a

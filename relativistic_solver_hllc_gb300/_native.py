@@ -117,7 +117,7 @@ _SIGNATURES = {
     "rts_write_simple_bin": (C.c_int, [C.c_char_p, _i64, _i64, _vp]),
     "rts_partition": (C.c_int, [C.c_int, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
     "rts_set_tuning": (C.c_int, [_vp, C.c_int, C.c_int]),
-    "rts_flush_period": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+    "rts_flush_period": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "rts_autotune": (C.c_int, [_vp, _i64, C.c_int, C.c_int, _i64, C.POINTER(C.c_int), _dp, C.POINTER(C.c_int), _dp,
                                C.c_int, C.POINTER(C.c_int)]),
     "rts_autotune_save": (C.c_int, [_vp, C.c_char_p]),
@@ -591,10 +591,11 @@ class Context:
     def set_tuning(self, key: int, value: int):
         self._check(self.lib.rts_set_tuning(self.h, int(key), int(value)), "rts_set_tuning")
 
-    def flush_period(self) -> int:
-        """K-slices per FP32 drain that the tensor-core calls use (RTS_TUNE_FLUSH or automatic)."""
+    def flush_period(self, precision="fp16x3") -> int:
+        """K-slices per FP32 drain that the tensor-core calls at `precision` use (RTS_TUNE_FLUSH or automatic)."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         v = C.c_int()
-        self._check(self.lib.rts_flush_period(self.h, C.byref(v)), "rts_flush_period")
+        self._check(self.lib.rts_flush_period(self.h, prec, C.byref(v)), "rts_flush_period")
         return v.value
 
     def autotune(self, M: int, precision="fp16x3", flush: int = 0, cells: int = 0):

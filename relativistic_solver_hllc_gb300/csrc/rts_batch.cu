@@ -105,7 +105,7 @@ int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* i
     if (rc != RTS_OK) return rc;
 
     GProb* p = nullptr;
-    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g);
+    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g, d->precision);
     rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), flush, d->bn, true, &p, st);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
@@ -121,6 +121,7 @@ int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* i
     }
     rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->mode, p->rs, p->rows_pad, p->a[0], st,
                               p->part != nullptr);
+    if (rc == RTS_OK) rc = rts_group_reset_energy(ctx, p, st);
     if (rc == RTS_OK && sync) {
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = rts_fail(ctx, RTS_ERR_CUDA, "rts_batch_add: %s", cudaGetErrorString(e));
@@ -291,7 +292,7 @@ extern "C" int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc*
     rc = rts_launch_weights_raw(ctx, d_xyz, d_area, (int)M, 0, (int)M, full_area, d->phase, d->g, W, st);
     if (rc != RTS_OK) return rc;
     GProb* p = nullptr;
-    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g);
+    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g, d->precision);
     rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), flush, d->bn, true, &p);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
@@ -304,6 +305,7 @@ extern "C" int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc*
     if (rc == RTS_OK && e == cudaSuccess)
         rc = rts_pp_rows_from_f32(ctx, stage, N, (int)M, rows, (int)p->kpad, p->B, p->mode, p->rs, p->rows_pad,
                                   p->a[0], st, p->part != nullptr);
+    if (rc == RTS_OK && e == cudaSuccess) rc = rts_group_reset_energy(ctx, p, st);
     if (rc == RTS_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
     int64_t new_id = 0;
     rts_group_attach(batch, p, &new_id);

@@ -884,10 +884,12 @@ int rts_get_precision(const rts_ctx* ctx, int* precision)
     return RTS_OK;
 }
 
-int rts_flush_period(const rts_ctx* ctx, int* flush)
+int rts_flush_period(const rts_ctx* ctx, int precision, int* flush)
 {
     if (!ctx || !flush) return RTS_ERR_INVALID_ARGUMENT;
-    *flush = rts_ctx_flush(ctx);
+    if (precision != RTS_PREC_BF16X3 && precision != RTS_PREC_FP16X3 && precision != RTS_PREC_TF32X3)
+        return RTS_ERR_INVALID_ARGUMENT;
+    *flush = rts_ctx_flush(ctx, precision);
     return RTS_OK;
 }
 

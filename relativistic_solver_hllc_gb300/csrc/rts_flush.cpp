@@ -12,6 +12,14 @@
 // 1/8 of the column (then the extra loss stays below ~7e-8): smooth kernels
 // (Thomson, Henyey-Greenstein with small g) on enough directions.  Peaked
 // kernels, small direction sets and caller-supplied W drain every slice.
+//
+// TF32x3 slices hold 16 in-directions (kind::tf32 multiplies 8 per MMA), so
+// its drain count per in-direction is twice FP16's at the same period, and
+// the round-to-nearest FP32 additions of the drains -- a random walk of
+// about sqrt(drains)/6 ulps of the sum -- dominate its error instead; it
+// drains every two slices (32 in-directions, the FP16x3 setting for peaked
+// kernels), measured within 1e-6 on peaked and smooth kernels alike where
+// one slice per drain reached 1.1e-6 at M = 1202.
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -19,8 +27,9 @@
 #include "rts_internal.h"
 
 int rts_auto_flush(const double* xyz, const double* area, int64_t M, double full_area, int64_t k0, int64_t k1,
-                   int phase, double g)
+                   int phase, double g, int precision)
 {
+    if (precision == RTS_PREC_TF32X3) return 2;
     if (phase != RTS_PHASE_THOMSON && phase != RTS_PHASE_HG) return 1;
     if (!xyz || !area || M <= 0 || k1 <= k0) return 1;
     const double pi = 3.14159265358979323846264338327950288;

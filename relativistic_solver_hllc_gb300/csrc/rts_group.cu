@@ -112,6 +112,7 @@ void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
     rts_pfree(ctx, p->vrow, (size_t)((p->kpad + 1) * 4), st);
     rts_pfree(ctx, p->part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), st);
     rts_pfree(ctx, p->delta, (size_t)(p->rows_pad * 4), st);
+    rts_pfree(ctx, p->ex, (size_t)(p->rows_pad * 8), st);
     delete p;
 }
 
@@ -153,7 +154,7 @@ float rts_group_bias(const rts_ctx* ctx, int, int)
 
 int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles)
 {
-    return (kpad + 1) * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 4;
+    return (kpad + 1) * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 12;
 }
 
 // Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
@@ -236,6 +237,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
         GP_ALLOC(vrow, (size_t)((p->kpad + 1) * 4), "W row sums");
         GP_ALLOC(part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), "energy partial sums");
         GP_ALLOC(delta, (size_t)(p->rows_pad * 4), "energy corrections");
+        GP_ALLOC(ex, (size_t)(p->rows_pad * 8), "conserved sums");
     }
 #undef GP_ALLOC
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
@@ -243,7 +245,6 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
     rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs, st);
     if (rc == RTS_OK && p->vrow) rc = rts_pp_row_sums(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, p->vrow, st);
-    if (rc == RTS_OK && p->delta) rc = rts_group_reset_energy(ctx, p, st);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->units, p->bn);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->units, G_BM);
     if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->units, G_BM);
@@ -263,6 +264,10 @@ int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st)
 {
     if (!p->delta) return RTS_OK;
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->delta, 0, (size_t)(p->rows_pad * 4), st));
+    group_energy_init_kernel<<<(unsigned)((p->rows + 127) / 128), 128, 0, st>>>(p->a[p->cur], p->rows, (int)p->kpad,
+                                                                             (int)p->M, p->mode, p->vrow, p->rs, p->ex);
+    RTS_CHECK_LAUNCH(ctx, "group_energy_init_kernel");
+    ctx->launches++;
     return RTS_OK;
 }
 
@@ -361,11 +366,13 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.a[0] = p->a[0];
     g.a[1] = p->a[1] ? p->a[1] : p->a[0];
     g.resid = b->d_resid + i;
-    // RTS_TUNE_BIAS -1 switches the conservation-based correction off
-    const bool energy = p->part != nullptr && ctx->split_bias >= 0;
+    // RTS_TUNE_BIAS -1 switches the conservation-based correction off; it
+    // applies to relaxed steps (a step without relaxation leaves the input)
+    const bool energy = p->part != nullptr && ctx->split_bias >= 0 && relaxes(p, relax);
     g.vrow = energy ? p->vrow : nullptr;
     g.part = energy ? reinterpret_cast<int4*>(p->part) : nullptr;
     g.delta = energy ? p->delta : nullptr;
+    g.ex = energy ? p->ex : nullptr;
     g.rsb = p->rs;
     p->slot = (int)i;
     tiles += p->m_tiles * p->n_tiles;

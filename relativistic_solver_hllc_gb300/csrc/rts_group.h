@@ -38,6 +38,7 @@ struct GProb {
     float* vrow = nullptr;   // [kpad + 1] v_j = sum_k W[j][k]; [kpad]: the quantum scale of the partial sums
     void* part = nullptr;    // [n_tiles * 4][rows_pad] int4 per-slot partial sums of a step (fixed point)
     float* delta = nullptr;  // [rows_pad] per-row correction of the next step
+    double* ex = nullptr;    // [rows_pad] sum_j v_j x_j of the current input (fixed-point quanta)
     alignas(64) unsigned char maps[3][128];
     alignas(64) unsigned char rmaps[2][128];  // relaxation boxes of a[0], a[1]
 };
@@ -80,5 +81,7 @@ void rts_group_invalidate(rts_batch* b);
 float rts_group_bias(const rts_ctx* ctx, int mode, int flush);
 // Bytes of the energy-correction buffers of an iterative problem.
 int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles);
-// Clears the per-row corrections (a restarted iteration starts uncorrected).
+// Clears the per-row corrections (a restarted iteration starts uncorrected)
+// and computes sum_j v_j x_j of the current split input: after the rows of
+// the problem's input were written.
 int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st);

@@ -41,12 +41,14 @@
 // by an amount that depends on how the partial sums grow inside an MMA) with
 // a conserved quantity instead of a measured constant: for any W,
 //     sum_k (W^T I)_k = sum_j v_j I_j,    v_j = sum_k W[j][k]  (FP64, once).
-// Every relaxed step writes, per cell and per epilogue warp, the two partial
-// sums -- of the raw integrals it produced and of v_j times the split
-// intensities it read (the values the tensor core multiplied) -- into
-// per-slot arrays; group_energy_kernel adds the slots and stores each cell's
-// delta = E_exact / E_tensor - 1, and the next step scales that cell's
-// integrals by (1 + delta).  This removes the cell's isotropic bias, the part
+// E_exact of a step's input needs no pass over it: the relaxation makes the
+// next input x' = x/2 + rs S/2, so E_exact' = E_exact/2 + rs (sum_j v_j S_j)/2,
+// and the first input's E_exact is computed once at set-up
+// (group_energy_init_kernel).  Every relaxed step writes, per cell and per
+// epilogue warp, the partial sums of its raw integrals and of v_j S_j into
+// per-slot arrays; group_energy_kernel adds the slots, stores each cell's
+// delta = E_exact / E_tensor - 1 and advances E_exact, and the next step
+// scales that cell's integrals by (1 + delta).  This removes the cell's isotropic bias, the part
 // that a relaxed iteration would otherwise compound step after step.  The
 // partial sums are exact fixed-point numbers: each block of 8 columns is
 // summed in FP32 in column order and rounded to a multiple of a per-row
@@ -116,7 +118,8 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     // energy-conservation correction of relaxed steps (null: none)
     const float* vrow;    // [kpad + 1] v_j = sum_k W[j][k], 0 past M; vrow[kpad] = q0 (below)
     int4* part;           // [n_tiles * 4][rows_pad] per-slot partials in quanta (high, low parts):
-                          // sum_j v_j x_j, then sum_k raw_k
+                          // sum_j v_j rs S_j, then sum_k raw_k
+    double* ex;           // [rows_pad] sum_j v_j x_j of the current input, in quanta
     float* delta;         // [rows_pad] per-cell correction of the next step (0: none yet)
     const float* rsb;     // [rows_pad] power of two with rsb * 2 max(|Ibar|, |B|) < 2^14 (all modes)
 };
@@ -165,8 +168,7 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
 // past `nk` become zero (the padding of the split rows).  Returns true when
 // an FP16 value leaves the range the row scale allows.
 template <bool kFp16>
-__device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk,
-                                       const float* vr, float& eb)
+__device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)[8], float hrsc, int nk)
 {
     const uint4 rh = *hp, rl = *lp;
     const uint32_t hw[4] = {rh.x, rh.y, rh.z, rh.w};
@@ -176,10 +178,6 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
         const float2 i2 = rts_ptx::join2_any(kFp16, hw[j >> 1], lw[j >> 1]);
-        if (vr) {  // the split values the tensor core multiplied, weighted by v_j
-            if (j < nk) eb = fmaf(vr[j], i2.x, eb);
-            if (j + 1 < nk) eb = fmaf(vr[j + 1], i2.y, eb);
-        }
         const float x0 = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * i2.x) : 0.0f;
         const float x1 = (j + 1 < nk) ? fmaf(snew[j + 1], hrsc, 0.5f * i2.y) : 0.0f;
         if (kFp16) amax = fmaxf(amax, fmaxf(fabsf(x0), fabsf(x1)));
@@ -191,15 +189,13 @@ __device__ __forceinline__ bool relax8(uint4* hp, uint4* lp, const float (&snew)
 }
 
 // The same for 4 columns of a split TF32 row (hi and lo as FP32, no scale).
-__device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk,
-                                            const float* vr, float& eb)
+__device__ __forceinline__ void relax4_tf32(float4* hp, float4* lp, const float* snew, float hrsc, int nk)
 {
     const float4 h = *hp, l = *lp;
     const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
     float nh[4], nl[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        if (vr && j < nk) eb = fmaf(vr[j], hv[j] + lv[j], eb);
         const float x = (j < nk) ? fmaf(snew[j], hrsc, 0.5f * (hv[j] + lv[j])) : 0.0f;
         rts_ptx::split_tf32(x, nh[j], nl[j]);
     }
@@ -452,14 +448,15 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const int64_t grp = in_row ? r / Nc : 0;
             const int64_t cc = in_row ? r - grp * Nc : 0;
             const bool fp16 = P.fp16 != 0;
-            const bool relax = P.relax != 0, residual = P.residual != 0;
+            // the energy instantiation runs relaxed source-iteration steps only
+            const bool relax = kEnergy || P.relax != 0, residual = kEnergy || P.residual != 0;
             const float* __restrict__ cs_inv = P.cs_inv;
-            const bool has_B = P.B != nullptr;
+            const bool has_B = kEnergy || P.B != nullptr;
             const float lam = (in_row && has_B) ? P.lam[grp] : 1.0f;
             const float lr = lam * ((fp16 && in_row) ? P.rs_inv[r] : 1.0f);
             const float bterm = (in_row && has_B) ? (1.0f - lam) * P.B[r] : 0.0f;
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
-            const bool want_rel = relax && (kEnergy || P.S64 == nullptr);  // relax implies Mout == M <= kpad
+            const bool want_rel = kEnergy || (relax && P.S64 == nullptr);  // relax implies Mout == M <= kpad
             // energy-conservation correction (relaxed steps): this cell's delta
             // from the previous step; the partial sums of this one.  `ewarp`
             // is uniform over the warp (the shuffles of v_j need every lane).
@@ -467,7 +464,9 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float qrow = (ewarp && in_row) ? energy_scale(P, r, fp16) : 0.0f;
             const bool cons = qrow > 0.0f;
             const float bias = P.bias + (cons ? P.delta[r] : 0.0f);
-            int xh = 0, xl = 0, th = 0, tl = 0;  // fixed-point partial sums (sum_j v_j x_j, sum_k raw_k)
+            // the sum of v_j S_j in the units of x (scaled by rs in FP16 mode)
+            const float qv = fp16 ? qrow * 2.0f * hrsc : qrow;
+            int xh = 0, xl = 0, th = 0, tl = 0;  // fixed-point partial sums (sum_j v_j rs S_j, sum_k raw_k)
             float vp0 = 0.0f, vp1 = 0.0f;        // v_j of this warp's columns kbase + 2 lane, + 1
             const int kbase = n_tile * bn + sw * cs;
             if (ewarp) {
@@ -566,6 +565,15 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     }
                     // blocks of 8 columns start at multiples of 8 of the out-directions
                     if (kEnergy && cons && live_k) fixed_add(eb * qrow, th, tl);
+                    if (kEnergy && ewarp) {  // sum_j v_j S_j of these columns (every lane shuffles)
+                        float ev = 0.0f;
+    #pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const float vj = __shfl_sync(0xffffffffu, (j & 1) ? vp1 : vp0, (e0 + j) >> 1);
+                            if (j < nk) ev = fmaf(vj, snew[j], ev);
+                        }
+                        if (cons && live_k) fixed_add(ev * qv, xh, xl);
+                    }
                     if (live_k) {
                         if (S64) {
                             double* dp = S64 + (int64_t)k0 * ld;
@@ -590,7 +598,6 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     // place (rows outside the problem stay unchanged), store the box
                     // into the other ping-pong buffer
                     bool stop = false;
-                    float xe = 0.0f;  // sum_j v_j x_j of these 8 columns
                     for (int ui = 0; ui < 8 / ucols; ++ui) {
                         const int u = e0 / ucols + ui;
                         if (u >= u_real) break;
@@ -604,26 +611,17 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         }
                         uint8_t* rb = rbuf + b * 1024u;
                         const int nku = min(ucols, Mout - (kbase + u * ucols));
-                        // v_j of the unit's columns, from the lanes holding them (all lanes shuffle)
-                        float vr[ucols];
-                        if (kEnergy && ewarp) {
-    #pragma unroll
-                            for (int j = 0; j < ucols; ++j)
-                                vr[j] = __shfl_sync(0xffffffffu, (j & 1) ? vp1 : vp0, (u * ucols + j) >> 1);
-                        }
                         if (in_row) {
-                            const float* vrp = (kEnergy && cons) ? vr : nullptr;
                             if (tf32) {
                                 relax4_tf32(reinterpret_cast<float4*>(rb + 16 * lane),
-                                            reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku,
-                                            vrp, xe);
+                                            reinterpret_cast<float4*>(rb + 512 + 16 * lane), snew + 4 * ui, hrsc, nku);
                             } else {
                                 uint4* hp = reinterpret_cast<uint4*>(rb + 16 * lane);
                                 uint4* lp = reinterpret_cast<uint4*>(rb + 512 + 16 * lane);
                                 if (fp16)
-                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku, vrp, xe);
+                                    overflow |= relax8<true>(hp, lp, snew, hrsc, nku);
                                 else
-                                    relax8<false>(hp, lp, snew, hrsc, nku, vrp, xe);
+                                    relax8<false>(hp, lp, snew, hrsc, nku);
                             }
                         }
                         fence_proxy_async_smem();
@@ -640,7 +638,6 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                         ok = false;
                         break;
                     }
-                    if (kEnergy && cons) fixed_add(xe * qrow, xh, xl);  // the same 8-column blocks
                 }
             };
             if (P.tf32)
@@ -682,21 +679,52 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
     const int64_t ld = P.m_tiles * (int64_t)G_BM;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.rows;
          r += (int64_t)gridDim.x * blockDim.x) {
-        long long ex = 0, et = 0;  // exact: in units of 2^-22 of the row's scale
+        long long ev = 0, et = 0;  // exact: in units of 2^-22 of the row's quantum
         for (int nt = 0; nt < P.n_tiles; ++nt)
             for (int cs = 0; cs < 4; ++cs) {
                 if (P.sw * cs >= P.bn) continue;  // a column slice without columns
                 const int4 v = P.part[((int64_t)nt * 4 + cs) * ld + r];
-                ex += ((long long)v.x << 22) + v.y;
+                ev += ((long long)v.x << 22) + v.y;
                 et += ((long long)v.z << 22) + v.w;
             }
+        const double q22 = 1.0 / 4194304.0;  // the slots' units, in quanta
+        const double ex = P.ex[r];           // sum_j v_j x_j of this step's input, in quanta
         float d = 0.0f;
-        if (ex > 0 && et > 0) {
-            const double g = (double)ex / (double)et - 1.0;
+        if (ex > 0.0 && et > 0) {
+            const double g = ex / ((double)et * q22) - 1.0;
             if (fabs(g) < 1e-4) d = (float)g;
         }
         P.delta[r] = d;
+        // the next input is x / 2 + rs S / 2
+        P.ex[r] = 0.5 * ex + 0.5 * ((double)ev * q22);
     }
+}
+
+// sum_j v_j x_j of every row of the current split input, in the quanta of
+// energy_scale (FP64, once per set-up of an iteration): the split values
+// joined as the tensor core multiplies them (hi + lo).
+__global__ void group_energy_init_kernel(const uint16_t* __restrict__ A, int64_t rows, int kpad, int M, int mode,
+                                         const float* __restrict__ vrow, const float* __restrict__ rs, double* ex)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    float q = vrow[kpad] * (mode == 1 ? 1.0f : rs[r]);
+    if (!(q > 0.0f && q < 3.0e38f)) q = 0.0f;
+    double s = 0.0;
+    if (mode == 2) {
+        const float* row = reinterpret_cast<const float*>(A + r * 4 * (int64_t)kpad);
+        for (int j = 0; j < M; ++j) {
+            const int h = (j >> 4) * 32 + (j & 15);
+            s += (double)vrow[j] * (double)(row[h] + row[h + 16]);
+        }
+    } else {
+        const uint16_t* row = A + r * 2 * (int64_t)kpad;
+        for (int j = 0; j < M; ++j) {
+            const int64_t h = rts_ptx::ilv_hi(j);
+            s += (double)vrow[j] * (double)rts_ptx::join_any(mode == 1, row[h], row[h + 32]);
+        }
+    }
+    ex[r] = s * (double)q;
 }
 
 // Flip the ping-pong Ibar buffer of every problem whose relaxed step ended in

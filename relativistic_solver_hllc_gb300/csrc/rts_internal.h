@@ -241,10 +241,10 @@ int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaSt
 // W is smooth enough that the longer truncation chains stay far below the
 // 1e-6 budget, else 1 (rts_flush.cpp).
 int rts_auto_flush(const double* xyz, const double* area, int64_t M, double full_area, int64_t k0, int64_t k1,
-                   int phase, double g);
-// The context's drain period: RTS_TUNE_FLUSH when set, else rts_auto_flush of
-// its directions, local out-directions and phase kernel.
-int rts_ctx_flush(const rts_ctx* ctx);
+                   int phase, double g, int precision);
+// The context's drain period at a precision: RTS_TUNE_FLUSH when set, else
+// rts_auto_flush of its directions, local out-directions and phase kernel.
+int rts_ctx_flush(const rts_ctx* ctx, int precision);
 
 // Tensor-core path (rts_split.cu).
 int rts_tuned_bn(const rts_ctx* ctx, int64_t M, int mode, int flush);

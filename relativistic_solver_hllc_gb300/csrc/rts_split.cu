@@ -13,11 +13,11 @@
 #include "rts_group.h"
 #include "rts_internal.h"
 
-int rts_ctx_flush(const rts_ctx* ctx)
+int rts_ctx_flush(const rts_ctx* ctx, int precision)
 {
     if (ctx->split_flush > 0) return ctx->split_flush;
     return rts_auto_flush(ctx->h_xyz.data(), ctx->h_area.data(), ctx->M, ctx->full_area, ctx->out_start, ctx->out_end,
-                          ctx->phase, ctx->phase_g);
+                          ctx->phase, ctx->phase_g, precision);
 }
 
 namespace {
@@ -28,7 +28,7 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
 {
     const int mode = rts_split_mode(precision);
     const int64_t N = ctx->N, Min = ctx->M, Mout = ctx->local();
-    const int flush = rts_ctx_flush(ctx);
+    const int flush = rts_ctx_flush(ctx, precision);
     GProb* p = nullptr;
     if (*pb) {
         p = rts_group_find(*pb, *id, nullptr);
@@ -164,7 +164,7 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
     const int mode = rts_split_mode(precision);
     const bool update = B_host != nullptr && lambda != 1.0;
     const int64_t N = ctx->N, M = ctx->M, Mout = ctx->local();
-    const int flush = rts_ctx_flush(ctx);
+    const int flush = rts_ctx_flush(ctx, precision);
     const int64_t tiles = (N + 127) / 128;
     const int nch = (int)std::min<int64_t>(RTS_HOST_CHUNKS, tiles);
     const int64_t csz = (tiles + nch - 1) / nch * 128;  // cells per range, whole 128-cell tiles
@@ -245,7 +245,7 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     rts_split_state& s = ctx->split;
     const int mode = rts_split_mode(precision);
     const int64_t N = ctx->N, M = ctx->M;
-    const int flush = rts_ctx_flush(ctx);
+    const int flush = rts_ctx_flush(ctx, precision);
     const int nch = 1;
     const int64_t csz = N;
     int rc;
@@ -288,7 +288,7 @@ int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int
     rts_split_state& s = ctx->split;
     const int mode = rts_split_mode(precision);
     const int64_t N = ctx->N, M = ctx->M, loc = ctx->local(), Mout = end - start;
-    const int flush = rts_ctx_flush(ctx);
+    const int flush = rts_ctx_flush(ctx, precision);
     int rc;
     GProb* p = s.slot[slot] ? rts_group_find(s.slot[slot], s.slot_id[slot], nullptr) : nullptr;
     if (p && (p->mode != mode || p->N != N || p->M != M || p->Mout != Mout || p->flush != flush ||

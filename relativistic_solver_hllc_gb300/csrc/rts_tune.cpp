@@ -54,7 +54,7 @@ extern "C" int rts_autotune(rts_ctx* ctx, int64_t M, int precision, int flush, i
         std::vector<double> xyz(3 * (size_t)M), area((size_t)M);
         double fa = 0.0;
         rts_synth_directions(M, xyz.data(), area.data(), &fa);
-        flush = rts_auto_flush(xyz.data(), area.data(), M, fa, 0, M, RTS_PHASE_THOMSON, 0.0);
+        flush = rts_auto_flush(xyz.data(), area.data(), M, fa, 0, M, RTS_PHASE_THOMSON, 0.0, precision);
     }
     RTS_REQUIRE(ctx, cells <= ((int64_t)1 << 26), RTS_ERR_INVALID_ARGUMENT, "rts_autotune: %lld cells",
                 (long long)cells);

@@ -12,7 +12,8 @@ the intensities (lognormal sigma 0.5 to 2), the direction count (146 to
 the number of relaxed steps (20, and 40 as the longest serving requests).
 
 * test_default_setting: every case at the library's default drain period
-  (automatic: two K-slices per drain only for smooth kernels);
+  (automatic: for FP16 two K-slices per drain only for smooth kernels, for
+  TF32 always two);
 * test_two_slices_per_drain_on_smooth_kernels: the benchmark's setting --
   two K-slices per drain forced -- on the Thomson cases, the ones the
   automatic choice gives it to.
@@ -71,7 +72,7 @@ def _check(ctx, prec, case, flush):
         ctx.set_phase(PHASE_HG, g)
     ctx.set_tuning(TUNE_FLUSH, flush)
     try:
-        used = ctx.flush_period()
+        used = ctx.flush_period(prec)
         ctx.synth_illum(SEED, 0.0, sigma)
         S_t = _run(ctx, prec, B, lam, steps)
         ctx.synth_illum(SEED, 0.0, sigma)
@@ -100,8 +101,9 @@ def _check(ctx, prec, case, flush):
 @pytest.mark.parametrize("case", CASES, ids=_case_id)
 def test_default_setting(ctx, prec, case):
     used = _check(ctx, prec, case, 0)
-    # the automatic drain period: two K-slices only for the smooth kernels
-    assert used == (2 if case in SMOOTH else 1)
+    # the automatic drain period: FP16 drains two K-slices (64 in-directions)
+    # only for the smooth kernels; TF32 always two (32 in-directions)
+    assert used == (2 if (case in SMOOTH or prec == "tf32x3") else 1)
 
 
 @pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
