@@ -704,6 +704,8 @@ def run_ours(args, rank, world, local):
                  "p99_over_isolated_p99": row.get("p99_vs_isolated_p99"),
                  "fifo_alone_p99_ms": row.get("fifo_alone_p99_ms"),
                  "fifo_alone_p99_over_isolated_p99": row.get("fifo_alone_p99_vs_isolated_p99"),
+                 "fifo_alone_p99_ms": row.get("fifo_alone_p99_ms"),
+                 "fifo_alone_p99_over_isolated_p99": row.get("fifo_alone_p99_vs_isolated_p99"),
                  "mean_queue_ms": row.get("mean_queue_ms"), "p99_queue_ms": row.get("p99_queue_ms"),
                  "throughput_cell_dir_iter_per_s": row["throughput_cell_dir_iter_per_s"],
                  "policy": sres["policy"], "window_s": args.serve_window,

@@ -235,6 +235,16 @@ def fifo_latencies(arrivals, service):
     return np.array(out)
 
 
+def fifo_latencies(arrivals, service):
+    """Latencies of requests served one at a time in arrival order, each for
+    its service time (seconds)."""
+    t, out = 0.0, []
+    for a, s in zip(arrivals, service):
+        t = max(t, a) + s
+        out.append(t - a)
+    return np.array(out)
+
+
 def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2.0, precision="fp16x3",
             policy=1, budget=0):
     cap = 120 * 10**9
@@ -308,6 +318,13 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
             row["isolated_p99_ms"] = float(np.percentile(iso, 99))
             row["p99_latency_over_isolated"] = float(np.percentile(ratio, 99))
             row["p99_vs_isolated_p99"] = st.p99_ms / float(np.percentile(iso, 99))
+            # the same arrivals through one server that runs each request alone
+            # for its isolated time, first come first served: what queueing
+            # alone costs at this load when requests gain nothing from sharing
+            # the device (a reference point for the measured p99)
+            fifo = fifo_latencies([r.arrival_s for r in reqs], iso / 1e3) * 1e3
+            row["fifo_alone_p99_ms"] = float(np.percentile(fifo, 99))
+            row["fifo_alone_p99_vs_isolated_p99"] = row["fifo_alone_p99_ms"] / float(np.percentile(iso, 99))
             # the same arrivals through one server that runs each request alone
             # for its isolated time, first come first served: what queueing
             # alone costs at this load when requests gain nothing from sharing

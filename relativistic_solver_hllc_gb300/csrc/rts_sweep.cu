@@ -351,6 +351,51 @@ __device__ inline void norm_term(double old, double cur, double& loc)
     }
 }
 
+// L2 eviction priorities of the sweep's loads.  Every direction reads the
+// cells' neighbour table and medium entries (48 B per cell, 32 MB at 663,552
+// cells: they fit in L2), while the items and attenuation factors (4 B and
+// 24 B per item) are read once per sweep.  Loads of the shared tables are
+// marked evict-last and the streams evict-first, so the streams do not push
+// the tables out of L2 (cache hints only: the values are the same).
+__device__ __forceinline__ uint64_t l2_policy_last()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int4 ld_hint(const int4* q, uint64_t pol)
+{
+    int4 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(q), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double2 ld_hint(const double2* q, uint64_t pol)
+{
+    double2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(q), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_hint(const double* q, uint64_t pol)
+{
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(q), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_hint(const uint32_t* q, uint64_t pol)
+{
+    uint32_t v;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(q), "l"(pol));
+    return v;
+}
+
 __device__ inline double pick(int g, double v0, double v1, double v2, double v3)
 {
     return g == 0 ? v0 : g == 1 ? v1 : g == 2 ? v2 : v3;
@@ -402,17 +447,18 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
             Il[id] = mean;
         }
     }
+    const uint64_t keep = l2_policy_last(), stream = l2_policy_first();
     for (int L = 0; L < ns; ++L) {
         const int i1 = steps[L + 1];
         for (int i = steps[L] + threadIdx.x; i < i1; i += SWEEP_THREADS) {
-            const uint32_t w = items[i];
+            const uint32_t w = ld_hint(items + i, stream);
             const int64_t c = w >> 8;
             const int f = (int)((w >> 6) & 3u);
             const double2 f01 = *reinterpret_cast<const double2*>(Il + 4 * c);
             const double2 f23 = *reinterpret_cast<const double2*>(Il + 4 * c + 2);
-            const int4 pr = *reinterpret_cast<const int4*>(a.pairs + 4 * c);
-            const double2 m01 = *reinterpret_cast<const double2*>(a.med + 4 * c);
-            const double2 m23 = *reinterpret_cast<const double2*>(a.med + 4 * c + 2);
+            const int4 pr = ld_hint(reinterpret_cast<const int4*>(a.pairs + 4 * c), keep);
+            const double2 m01 = ld_hint(reinterpret_cast<const double2*>(a.med + 4 * c), keep);
+            const double2 m23 = ld_hint(reinterpret_cast<const double2*>(a.med + 4 * c + 2), keep);
             const double Sc = Sd[c];
             const CellTerms cell = cell_terms(a.md, unit_i, unit_s, m01.x, m01.y, m23.x, m23.y, Sc);
             const double* sr = recs + 3 * (int64_t)i;
@@ -430,7 +476,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
                     inb[m] = sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.md.radius;
                 }
                 if (kAtt == 2) {
-                    e3[m] = att[3 * (int64_t)i + m];
+                    e3[m] = ld_hint(att + 3 * (int64_t)i + m, stream);
                 } else {
                     const CellTerms t =
                         inb[m] ? cell_terms(a.md, unit_i, unit_s, a.ball[0], a.ball[1], a.ball[2], a.ball[3], Sc)
