@@ -153,12 +153,16 @@ int rts_get_precision(const rts_ctx* ctx, int* precision);
  * [start, end) to host_out + start*N (host_out NULL: the pinned host
  * scattering array).  The reference offsets the copy by `start` elements,
  * which is right only for start == 0; this entry point uses start*N.  Work on
- * a stream other than RTS_STREAM_SCATTERING_1 is ordered after the Illum
- * copies queued there.  Calls on different streams may overlap, as the
- * reference's pair on scattering streams 1 and 2 does
- * (solve_module/illum/Illum_async.cpp:1019-1020): at a tensor precision each
- * stream slot has split operands of its own, and rows both calls cover
- * receive the same values from either. */
+ * a stream other than RTS_STREAM_SCATTERING_1 is ordered after the writes of
+ * the device Illum, W and scattering array queued there (the Illum copies of
+ * rts_send_illum_async among them), not after the integral calls queued
+ * there: calls on different streams overlap, as the reference's pair on
+ * scattering streams 1 and 2 does (solve_module/illum/Illum_async.cpp:
+ * 1019-1020).  At a tensor precision each stream slot has split operands of
+ * its own, and rows both calls cover receive the same values from either.
+ * As in the reference, Illum copies queued after a call on another stream
+ * are not ordered after that call: synchronise the streams
+ * (rts_sync_stream) before rewriting the Illum. */
 int rts_scattering_async(rts_ctx* ctx, int64_t start, int64_t end, int stream, double* host_out);
 
 /* Replaces CalculateIntScattering (cuda/cuda_solve.cu:153-170): copies

@@ -115,11 +115,31 @@ static void free_grid(rts_ctx* ctx)
     ctx->h_illum = ctx->h_S = nullptr;
     ctx->N = ctx->M = 0;
     ctx->out_start = ctx->out_end = 0;
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     ctx->solve_has_prev = false;
 }
 
 static bool valid_stream(int s) { return s >= 0 && s < RTS_STREAM_COUNT; }
+
+// Orders an integral call on `stream` after the writes of its device inputs
+// (the Illum copies and every other rewrite of the Illum, W or scattering
+// array queued on the scattering stream), but not after the integral calls
+// queued there since: the mark is recorded on the scattering stream at the
+// first integral call after such a write, before that call's own work.  The
+// reference's pair of calls on scattering streams 1 and 2
+// (solve_module/illum/Illum_async.cpp:1019-1020) then overlaps, one call's
+// D2H with the other's integral, as the reference's unordered streams do.
+static int after_input_writes(rts_ctx* ctx, int stream)
+{
+    cudaStream_t s1 = ctx->streams[RTS_STREAM_SCATTERING_1];
+    if (!ctx->ev_inputs) RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_inputs, cudaEventDisableTiming));
+    if (!ctx->inputs_marked) {
+        RTS_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_inputs, s1));
+        ctx->inputs_marked = true;
+    }
+    if (stream != RTS_STREAM_SCATTERING_1) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->streams[stream], ctx->ev_inputs, 0));
+    return RTS_OK;
+}
 
 // Orders stream slot `stream` after the work already queued on the
 // scattering stream (where the Illum copies go), with the context's event of
@@ -244,6 +264,7 @@ int rts_ctx_destroy(rts_ctx* ctx)
         if (ctx->ev_order[i]) cudaEventDestroy(ctx->ev_order[i]);
         if (ctx->ev_sync[i]) cudaEventDestroy(ctx->ev_sync[i]);
     }
+    if (ctx->ev_inputs) cudaEventDestroy(ctx->ev_inputs);
     delete ctx;
     return RTS_OK;
 }
@@ -352,7 +373,7 @@ int rts_set_phase(rts_ctx* ctx, int phase, double g)
                 "rts_set_phase: HG asymmetry g=%g outside (-1,1)", g);
     ctx->phase = phase;
     ctx->phase_g = g;
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     ctx->w_version++;
     return rts_launch_weights(ctx);
 }
@@ -365,7 +386,7 @@ int rts_set_weights(rts_ctx* ctx, const double* W)
     RTS_CUDA_TRY(ctx, cudaMemcpy(ctx->d_W, W, rts_bytes<double>(ctx->M * ctx->local()),
                                  cudaMemcpyHostToDevice));
     ctx->phase = RTS_PHASE_CUSTOM;
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     ctx->w_version++;
     return RTS_OK;
 }
@@ -385,7 +406,7 @@ int rts_send_illum_async(rts_ctx* ctx, int64_t size, int64_t shift_dev, int64_t 
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_illum + shift_dev, illum_host + shift_host,
                                       rts_bytes<double>(size), cudaMemcpyHostToDevice,
                                       ctx->streams[RTS_STREAM_SCATTERING_1]));
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     return RTS_OK;
 }
 
@@ -398,7 +419,7 @@ int rts_copy_illum(rts_ctx* ctx, int64_t size, const double* illum_host)
                 "rts_copy_illum: size %lld exceeds the device Illum", (long long)size);
     RTS_CUDA_TRY(ctx, cudaMemcpy(ctx->d_illum, illum_host, rts_bytes<double>(size),
                                  cudaMemcpyHostToDevice));
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     return RTS_OK;
 }
 
@@ -426,8 +447,7 @@ int rts_scattering_async(rts_ctx* ctx, int64_t start, int64_t end, int stream, d
                 (long long)start, (long long)end, (long long)ctx->local());
     if (start == end) return RTS_OK;
     cudaStream_t st = ctx->streams[stream];
-    // Illum copies go on stream 0; a later stream must see them.
-    int rc = after_scattering_stream(ctx, stream);
+    int rc = after_input_writes(ctx, stream);
     if (rc != RTS_OK) return rc;
     if (ctx->call_precision == RTS_PREC_FP64)
         rc = rts_launch_scatter_fp64(ctx, start, end, st, nullptr, 0.0, false, false);
@@ -448,13 +468,13 @@ int rts_scattering(rts_ctx* ctx, const double* illum_host, double* host_out)
     const double* src = illum_host ? illum_host : ctx->h_illum;
     double* dst = host_out ? host_out : ctx->h_S;
     if (ctx->call_precision != RTS_PREC_FP64) {  // the bare integral at that precision, pipelined over cell ranges
-        ctx->solve_ready = false;
+        rts_inputs_changed(ctx);
         return rts_split_host_call(ctx, ctx->call_precision, src, nullptr, 1.0, dst);
     }
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_illum, src, rts_bytes<double>(ctx->M * ctx->N * 4),
                                       cudaMemcpyHostToDevice, st));
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     int rc = rts_launch_scatter_fp64(ctx, 0, ctx->local(), st, nullptr, 0.0, false, false);
     if (rc != RTS_OK) return rc;
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(dst, ctx->d_S, rts_bytes<double>(ctx->local() * ctx->N),
@@ -473,7 +493,7 @@ int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
     RTS_REQUIRE(ctx, B_host || lambda == 1.0, RTS_ERR_INVALID_ARGUMENT,
                 "rts_scattering_update: B is required unless lambda == 1");
     if (precision == RTS_PREC_BF16X3 || precision == RTS_PREC_FP16X3 || precision == RTS_PREC_TF32X3) {
-        ctx->solve_ready = false;
+        rts_inputs_changed(ctx);
         return rts_split_host_call(ctx, precision, illum_host, B_host, lambda, S_host);
     }
     RTS_REQUIRE(ctx, precision == RTS_PREC_FP64, RTS_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
@@ -481,7 +501,7 @@ int rts_scattering_update(rts_ctx* ctx, int precision, const double* illum_host,
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_illum, illum_host,
                                       rts_bytes<double>(ctx->M * ctx->N * 4),
                                       cudaMemcpyHostToDevice, st));
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     const bool update = B_host != nullptr && lambda != 1.0;
     if (update)
         RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_B, B_host, rts_bytes<double>(ctx->N),
@@ -519,7 +539,7 @@ int rts_send_scattering(rts_ctx* ctx, int64_t start, int64_t end, int stream, co
                 "rts_send_scattering: [%lld,%lld) outside the %lld local out-directions", (long long)start,
                 (long long)end, (long long)ctx->local());
     if (start == end) return RTS_OK;
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_S + start * ctx->N, host + start * ctx->N,
                                       rts_bytes<double>((end - start) * ctx->N), cudaMemcpyHostToDevice,
                                       ctx->streams[stream]));
@@ -703,6 +723,7 @@ int rts_solve_setup(rts_ctx* ctx, int precision, const double* B_host, double la
     RTS_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_B, B_host, rts_bytes<double>(ctx->N),
                                       cudaMemcpyHostToDevice, st));
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_S, 0, rts_bytes<double>(ctx->M * ctx->N), st));
+    rts_inputs_written(ctx);  // S cleared; the steps relax the Illum
     ctx->solve_precision = precision;
     ctx->solve_lambda = lambda;
     ctx->solve_has_prev = false;
@@ -730,6 +751,7 @@ int rts_solve_step_async(rts_ctx* ctx, int relax)
     } else {
         rc = rts_split_step(ctx, relax != 0, st);
     }
+    rts_inputs_written(ctx);
     ctx->solve_has_prev = true;
     ctx->solve_steps++;
     return rc;
@@ -823,7 +845,7 @@ int rts_synth_illum(rts_ctx* ctx, uint64_t seed, double mu, double sigma, int in
 {
     if (!ctx) return RTS_ERR_INVALID_ARGUMENT;
     RTS_REQUIRE(ctx, ctx->d_illum, RTS_ERR_BAD_STATE, "rts_synth_illum before rts_init");
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     return rts_launch_synth(ctx, seed, mu, sigma, independent_faces);
 }
 

@@ -103,9 +103,9 @@ void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
     const size_t abytes = (size_t)(p->rows_pad * p->units * 2);
     rts_pfree(ctx, p->wc, (size_t)(p->mpad * p->units * 2), st);
     rts_pfree(ctx, p->cs, (size_t)(2 * p->mpad * 4), st);
-    rts_pfree(ctx, p->a[0], abytes, st);
+    if (!p->a_ext) rts_pfree(ctx, p->a[0], abytes, st);
     rts_pfree(ctx, p->a[1], abytes, st);
-    rts_pfree(ctx, p->rs, (size_t)(2 * p->rows_pad * 4), st);
+    if (!p->a_ext) rts_pfree(ctx, p->rs, (size_t)(2 * p->rows_pad * 4), st);
     rts_pfree(ctx, p->B, (size_t)(p->rows * 4), st);
     rts_pfree(ctx, p->lam, (size_t)(p->groups * 4), st);
     rts_pfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4), st);
@@ -192,8 +192,10 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
 // split into rows, tensor maps.  A rows, B and lambda are filled by the caller.
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev,
                           int ldw, int mode, int flush, int bn_override, bool iterative, GProb** out,
-                          cudaStream_t st)
+                          cudaStream_t st, uint16_t* ext_a, float* ext_rs)
 {
+    if ((ext_a != nullptr) != (ext_rs != nullptr) || (ext_a && (iterative || groups != 1)))
+        return rts_fail(b->ctx, RTS_ERR_INVALID_ARGUMENT, "shared split rows need a single evaluation of one group");
     const bool fp16 = mode == 1;
     rts_ctx* ctx = b->ctx;
     GProb* p = new GProb();
@@ -222,11 +224,17 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     const size_t abytes = (size_t)(p->rows_pad * p->units * 2);
     GP_ALLOC(wc, (size_t)(p->mpad * p->units * 2), "split W");
     GP_ALLOC(cs, (size_t)(2 * p->mpad * 4), "W column scales");
-    GP_ALLOC(a[0], abytes, "split Ibar");
+    if (ext_a) {
+        p->a_ext = true;
+        p->a[0] = ext_a;
+        p->rs = ext_rs;
+    } else {
+        GP_ALLOC(a[0], abytes, "split Ibar");
+        GP_ALLOC(rs, (size_t)(2 * p->rows_pad * 4), "Ibar row scales");
+    }
     if (iterative) {
         GP_ALLOC(a[1], abytes, "split Ibar (next)");
     }
-    GP_ALLOC(rs, (size_t)(2 * p->rows_pad * 4), "Ibar row scales");
     GP_ALLOC(B, (size_t)(p->rows * 4), "source B");
     GP_ALLOC(lam, (size_t)(p->groups * 4), "albedo");
     const bool energy = iterative && Mout == Min;
@@ -240,7 +248,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
         GP_ALLOC(ex, (size_t)(p->rows_pad * 8), "conserved sums");
     }
 #undef GP_ALLOC
-    RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
+    if (!ext_a) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
     if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
     rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs, st);

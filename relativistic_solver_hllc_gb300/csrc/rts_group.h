@@ -25,6 +25,7 @@ struct GProb {
     float* cs = nullptr;     // [2*mpad]: column scale, inverse
     uint16_t* a[2] = {nullptr, nullptr};  // [rows_pad][2*kpad] split Ibar rows (ping-pong)
     float* rs = nullptr;     // [2*rows_pad]: row scale, inverse
+    bool a_ext = false;      // a[0] and rs belong to the caller (shared rows), not freed here
     float* B = nullptr;      // [rows]
     float* lam = nullptr;    // [groups]
     float* S32 = nullptr;    // [groups][Mout][N] (source iteration)
@@ -49,8 +50,11 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
 int rts_group_batch_new(rts_ctx* ctx, rts_batch** out);
 void rts_group_batch_free(rts_batch* b);
 // buffers allocated and initialised on st (null: the scattering stream)
+// ext_a / ext_rs (single evaluations only): split Ibar rows and row scales the
+// caller owns and fills, laid out as this problem's own would be
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev, int ldw,
-                          int mode, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr);
+                          int mode, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr,
+                          uint16_t* ext_a = nullptr, float* ext_rs = nullptr);
 int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
 GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
 int rts_group_remove(rts_batch* b, int64_t id);

@@ -63,14 +63,32 @@ struct rts_split_state {
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
     cudaEvent_t ev_start = nullptr, ev_in[RTS_HOST_CHUNKS] = {}, ev_done[RTS_HOST_CHUNKS] = {};
     // reference-compatible asynchronous calls (rts_scattering_async) at a
-    // tensor precision: one one-problem batch per stream slot, each with its
-    // own split operands, so that calls queued on different streams at the
-    // same time (the reference's pair on scattering streams 1 and 2) never
-    // share a buffer they write
+    // tensor precision: one one-problem batch per stream slot (its split W
+    // rows of the slot's out-directions, its outputs), so that calls queued on
+    // different streams at the same time (the reference's pair on scattering
+    // streams 1 and 2) never share a buffer they write
     rts_batch* slot[RTS_STREAM_COUNT] = {};
     int64_t slot_id[RTS_STREAM_COUNT] = {};
     int64_t slot_start[RTS_STREAM_COUNT] = {};
     int64_t slot_w_version[RTS_STREAM_COUNT] = {};
+    int64_t slot_gen[RTS_STREAM_COUNT] = {};   // call_gen the slot's problem was built on
+    // ... and their split Ibar rows, which depend on the Illum only: one copy
+    // shared by the slots, prepared by a call and reused by the next call on
+    // each other slot while the inputs are unchanged (the pair)
+    uint16_t* call_a = nullptr;               // [rows_pad][units]
+    float* call_rs = nullptr;                 // [2*rows_pad] row scales, inverse
+    double* call_sums = nullptr;              // [M][N] FP64 face sums (staging)
+    unsigned long long* call_max = nullptr;   // [N] max |face mean| per cell (FP64 bits)
+    size_t call_a_bytes = 0, call_rs_bytes = 0, call_sums_bytes = 0, call_max_bytes = 0;
+    int call_mode = -1;
+    int64_t call_N = 0, call_M = 0;
+    int64_t call_gen = 0;                     // bumped when the shared buffers are reallocated
+    int64_t call_version = -1;                // inputs_version the rows were prepared from
+    int prep_slot = -1;                       // slot whose call prepared them
+    bool prep_served[RTS_STREAM_COUNT] = {};  // other slots that have reused them
+    cudaEvent_t ev_prep = nullptr;            // on the preparing slot's stream: rows ready
+    cudaEvent_t ev_use[RTS_STREAM_COUNT] = {};  // on each slot's stream: its contraction queued
+    bool use_recorded[RTS_STREAM_COUNT] = {};
 };
 
 // Device state of the transport sweep (rts_sweep.cu): the mesh, the
@@ -166,6 +184,9 @@ struct rts_ctx {
     int64_t solve_steps = 0;
     int call_precision = RTS_PREC_FP64;  // rts_scattering_async / rts_scattering (rts_set_precision)
     cudaEvent_t ev_order[RTS_STREAM_COUNT] = {};  // cross-stream ordering, one per waiting stream
+    cudaEvent_t ev_inputs = nullptr;  // on the scattering stream: the device inputs of the integral calls written
+    bool inputs_marked = false;       // ev_inputs covers every write of them queued so far
+    int64_t inputs_version = 0;       // bumped at every write of the device Illum, W or scattering array
     cudaEvent_t ev_sync[RTS_STREAM_COUNT] = {};   // rts_sync_stream deadlines
     rts_split_state split;
     int split_flush = 0;         // hi*hi drain period in stages (0: default)
@@ -217,6 +238,23 @@ int rts_launch_weights_raw(rts_ctx* ctx, const double* d_xyz, const double* d_ar
 
 // Operand preparation of the split-precision path (rts_prepass.cu).
 // Split formats of the tensor-core operands: mode 0 BF16, 1 FP16 (scaled), 2 TF32.
+// The device Illum, W or scattering array was (or is queued to be) written:
+// the next integral call on another stream must wait for the write, and
+// operands prepared from the old contents are stale.
+inline void rts_inputs_written(rts_ctx* ctx)
+{
+    ctx->inputs_marked = false;
+    ctx->inputs_version++;
+}
+
+// ... by a call other than the source iteration's own steps: the resident
+// iteration must be set up again as well.
+inline void rts_inputs_changed(rts_ctx* ctx)
+{
+    ctx->solve_ready = false;
+    rts_inputs_written(ctx);
+}
+
 inline int rts_split_mode(int precision) { return precision == RTS_PREC_FP16X3 ? 1 : precision == RTS_PREC_TF32X3 ? 2 : 0; }
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
                    uint16_t* Wc, float* cs, cudaStream_t st);
@@ -227,6 +265,14 @@ int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t
                            float* rs, int64_t npad, uint16_t* A, cudaStream_t st, bool bound = false);
 int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int64_t rows, int kpad, const float* B,
                          int mode, float* rs, int64_t rows_pad, uint16_t* A, cudaStream_t st, bool bound = false);
+// The rows of rts_pp_rows_from_faces (bit for bit) in two passes that read the
+// FP64 Illum once: FP64 face sums into the staging sums [M][N] with the
+// per-cell max |face sum| into cmax [N] (the bits of a non-negative double),
+// then the scales and the split from the staging; the FP64 pipe does only
+// the 3 adds of each sum.
+int rts_pp_rows_from_faces_staged(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad,
+                                  const double* B, int mode, float* rs, int64_t npad, uint16_t* A, double* sums,
+                                  unsigned long long* cmax, cudaStream_t st, bool bound = false);
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);

@@ -16,8 +16,10 @@
 //     into [2^13, 2^14), so hi + lo keeps 22 bits with 4x headroom to 65504;
 //   * the inverse (rows back to FP64 Ibar) for inspection.
 // All are HBM-bound: the Illum prepass reads 32 B and writes 4 B per
-// (cell, direction).  Transposes go through shared memory so both the
-// direction-major reads and the cell-major writes are coalesced.
+// (cell, direction); its staged form reads the 32 B once, writes and reads
+// back the 8 B FP64 face sum and writes the 4 B of rows.  Transposes go
+// through shared memory so both the direction-major reads and the
+// cell-major writes are coalesced.
 #include <cstdint>
 
 #include "rts_internal.h"
@@ -27,10 +29,12 @@ using namespace rts_ptx;
 
 namespace {
 
+// 2^(13 - ilogb(m)), within FP32's normal range (rows or columns whose
+// largest value is below 2^-113 or above 2^139 keep the nearest scale).
 __device__ __forceinline__ float pow2_scale(double m)
 {
     if (!(m > 0.0) || !isfinite(m)) return 1.0f;
-    return ldexpf(1.0f, 13 - ilogb(m));
+    return ldexpf(1.0f, max(-126, min(127, 13 - ilogb(m))));
 }
 
 // W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
@@ -139,6 +143,76 @@ __global__ void rowscale_faces_kernel(const double* __restrict__ illum, int64_t 
     rs[npad + c] = 1.0f / s;
 }
 
+// x * 2^k rounded to the nearest FP32 (ties to even), from the bit pattern
+// on the integer pipe: GB300's FP64 pipe issues about two instructions per SM
+// per cycle against 128 for FP32 / integer, and would bound a pass that
+// scaled and converted every value there.  Where x * 2^k is in FP32's normal
+// range the 52-bit mantissa keeps its top 23 bits, rounded on the 29 below
+// (a carry into the exponent is the correctly rounded result, up to
+// infinity); zeros, FP64 subnormals, FP32 subnormal or overflowing results
+// and NaN take ldexp and the hardware conversion.  Either way one rounding
+// of the exact product.
+__device__ __forceinline__ float pow2_scaled_to_f32(double x, int k)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((u >> 52) & 0x7FF);
+    const int ef = e + k - 1023 + 127;  // biased FP32 exponent of x * 2^k
+    if (e == 0 || e == 0x7FF || ef < 1 || ef > 254) return __double2float_rn(ldexp(x, k));
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    unsigned int f = ((unsigned int)ef << 23) | (unsigned int)(m >> 29);
+    const unsigned int rem = (unsigned int)m & 0x1FFFFFFFu;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ++f;
+    return __uint_as_float(f | ((unsigned int)(u >> 32) & 0x80000000u));
+}
+
+// Face sums of the face layout (FP64, the reference's order) into a
+// direction-major staging [M][N], and with cmax non-null the per-cell max
+// over the directions of |face sum| (FP64 bits: non-negative doubles order
+// like unsigned integers, so the max runs on the integer pipe and merges with
+// atomicMax; NaN is skipped, as fmax does in the row-scale pass above).  The
+// FP64 work is the 3 adds of the sum.  Thread per (cell, 32 directions): a
+// warp reads 1 KB and writes 256 B contiguous per direction, no transpose.
+__global__ void __launch_bounds__(256) face_sums_kernel(const double* __restrict__ illum, int64_t N, int64_t ld,
+                                                        int M, double* __restrict__ sums,
+                                                        unsigned long long* __restrict__ cmax)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const int j0 = blockIdx.y * 32;
+    const int j1 = min(M, j0 + 32);
+    unsigned long long mx = 0;
+#pragma unroll 8
+    for (int j = j0; j < j1; ++j) {
+        const double2* p = reinterpret_cast<const double2*>(illum + ((int64_t)j * ld + c) * 4);
+        const double2 a = __ldg(p), b = __ldg(p + 1);
+        double I = a.x;  // faces 0..3 in order (GET_FACE_TO_CELL), as face_mean
+        I += a.y;
+        I += b.x;
+        I += b.y;
+        sums[(int64_t)j * N + c] = I;
+        const unsigned long long ub = (unsigned long long)__double_as_longlong(I) & 0x7FFFFFFFFFFFFFFFull;
+        if (ub <= 0x7FF0000000000000ull && ub > mx) mx = ub;
+    }
+    if (cmax) atomicMax(cmax + c, mx);
+}
+
+// Row scales from the per-cell maxima of face_sums_kernel: the scale of
+// rowscale_faces_kernel (max_j |sum / 4| = max_j |sum| / 4 exactly; max is
+// order-free).
+__global__ void rowscale_from_max_kernel(const unsigned long long* __restrict__ cmax, int64_t N,
+                                         const double* __restrict__ B, float* __restrict__ rs, int64_t npad)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= npad) return;
+    float s = 1.0f;
+    if (c < N) {
+        const double m = B ? fabs(B[c]) : 0.0;
+        s = pow2_scale(2.0 * fmax(m, __longlong_as_double((long long)cmax[c]) / 4));
+    }
+    rs[c] = s;
+    rs[npad + c] = 1.0f / s;
+}
+
 // Row scales from direction-major FP32 Ibar [groups][M][N]: thread per row.
 __global__ void rowscale_f32_kernel(const float* __restrict__ ibar, int64_t N, int M, int64_t rows,
                                     const float* __restrict__ B, float* __restrict__ rs, int64_t rows_pad)
@@ -155,6 +229,21 @@ __global__ void rowscale_f32_kernel(const float* __restrict__ ibar, int64_t N, i
     }
     rs[r] = s;
     rs[rows_pad + r] = 1.0f / s;
+}
+
+// x * s rounded once to FP32 (s a power of two): an FP64 source multiplies
+// in FP64, an FP32 one in FP32 -- the same exact product, one rounding, and
+// no FP64 instruction for the FP32 sources.
+__device__ __forceinline__ float scaled_f32(double x, float s) { return (float)(x * (double)s); }
+__device__ __forceinline__ float scaled_f32(float x, float s) { return x * s; }
+// A staged face sum: its mean x / 4 times s, by the exponent arithmetic above
+// (s a normal power of two).
+struct FaceSum {
+    double x;
+};
+__device__ __forceinline__ float scaled_f32(FaceSum v, float s)
+{
+    return pow2_scaled_to_f32(v.x, (int)((__float_as_uint(s) >> 23) & 0xFF) - 127 - 2);
 }
 
 // Transpose-and-split through shared memory.  Tile: 32 in-directions x 64
@@ -175,7 +264,7 @@ __device__ __forceinline__ void split_tile(const Src& src, int64_t rows, int M, 
         for (int q = 0; q < 8; ++q) {
             const int jj = (t >> 6) + 4 * q;
             const int j = j0 + jj;
-            tile[rr][jj] = (r < rows && j < M) ? (float)(src(j, r) * (double)s) : 0.0f;
+            tile[rr][jj] = (r < rows && j < M) ? scaled_f32(src(j, r), s) : 0.0f;
         }
     }
     __syncthreads();
@@ -226,12 +315,26 @@ struct F32Src {
     const float* ibar;
     int64_t N;
     int M;
-    __device__ double operator()(int j, int64_t r) const
+    __device__ float operator()(int j, int64_t r) const
     {
         const int64_t g = r / N, c = r - g * N;
-        return (double)__ldg(ibar + (g * M + j) * N + c);
+        return __ldg(ibar + (g * M + j) * N + c);
     }
 };
+
+// The direction-major FP64 face sums of face_sums_kernel.
+struct SumSrc {
+    const double* sums;
+    int64_t N;
+    __device__ FaceSum operator()(int j, int64_t c) const { return FaceSum{__ldg(sums + (int64_t)j * N + c)}; }
+};
+
+__global__ void __launch_bounds__(256) split_sums_kernel(const double* __restrict__ sums, int64_t N, int M, int kpad,
+                                                         const float* __restrict__ rs, int mode,
+                                                         uint16_t* __restrict__ A)
+{
+    split_tile(SumSrc{sums, N}, N, M, kpad, rs, mode, A);
+}
 
 __global__ void __launch_bounds__(256) split_faces_kernel(const double* __restrict__ illum, int64_t N, int64_t ld,
                                                           int M, int kpad, const float* __restrict__ rs, int mode,
@@ -320,6 +423,29 @@ int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t
     dim3 grid((unsigned)((N + 63) / 64), (unsigned)(kpad / 32));
     split_faces_kernel<<<grid, 256, 0, st>>>(illum, N, ld, M, kpad, fp16 ? rs : nullptr, mode, A);
     RTS_CHECK_LAUNCH(ctx, "split_faces_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
+int rts_pp_rows_from_faces_staged(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad,
+                                  const double* B, int mode, float* rs, int64_t npad, uint16_t* A, double* sums,
+                                  unsigned long long* cmax, cudaStream_t st, bool bound)
+{
+    const bool fp16 = mode == 1;
+    const bool scaled = fp16 || bound;
+    if (scaled) RTS_CUDA_TRY(ctx, cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned long long), st));
+    face_sums_kernel<<<dim3((unsigned)((N + 255) / 256), (unsigned)((M + 31) / 32)), 256, 0, st>>>(
+        illum, N, ld, M, sums, scaled ? cmax : nullptr);
+    RTS_CHECK_LAUNCH(ctx, "face_sums_kernel");
+    ctx->launches++;
+    if (scaled) {
+        rowscale_from_max_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(cmax, N, B, rs, npad);
+        RTS_CHECK_LAUNCH(ctx, "rowscale_from_max_kernel");
+        ctx->launches++;
+    }
+    dim3 grid((unsigned)((N + 63) / 64), (unsigned)(kpad / 32));
+    split_sums_kernel<<<grid, 256, 0, st>>>(sums, N, M, kpad, fp16 ? rs : nullptr, mode, A);
+    RTS_CHECK_LAUNCH(ctx, "split_sums_kernel");
     ctx->launches++;
     return RTS_OK;
 }

@@ -1196,7 +1196,7 @@ extern "C" int rts_sweep(rts_ctx* ctx, int stream, double* norm)
     int rc = sweep_ready(ctx);
     if (rc != RTS_OK) return rc;
     cudaStream_t st = ctx->streams[stream];
-    ctx->solve_ready = false;  // the device Illum changes under a resident tensor-core iteration
+    rts_inputs_changed(ctx);  // the device Illum changes under a resident tensor-core iteration
     if ((rc = enqueue_sweep(ctx, st)) != RTS_OK) return rc;
     if (norm) return read_norm(ctx, st, norm);
     return RTS_OK;
@@ -1214,7 +1214,7 @@ extern "C" int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double
     int rc = sweep_ready(ctx);
     if (rc != RTS_OK) return rc;
     cudaStream_t st = ctx->streams[RTS_STREAM_SCATTERING_1];
-    ctx->solve_ready = false;
+    rts_inputs_changed(ctx);
     int64_t count = 0;
     double norm = -1.0;
     do {

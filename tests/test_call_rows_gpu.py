@@ -1,0 +1,72 @@
+"""The operand preparation of the asynchronous integral calls at a tensor
+precision (one pass over the face-layout Illum into FP64 face sums and
+per-cell maxima, then the scaled conversion to FP32 on the integer pipe and
+the split; the rows shared by the stream slots) gives the rows of the direct
+preparation bit for bit: rts_scattering_async and rts_scattering (whose
+host-buffer pipeline prepares each cell range directly from the FP64 faces)
+return identical S.
+
+The Illum holds, besides lognormal values, face sums that sit exactly on an
+FP32 rounding tie after the division by 4 (ties to even, both parities),
+zeros, values whose quarter is subnormal in FP32 (the conversion's fallback),
+negative values and a wide spread of magnitudes within cells."""
+import numpy as np
+import pytest
+
+import oracle
+from relativistic_solver_hllc_gb300 import STREAM_SCATTERING_1, STREAM_SCATTERING_2
+
+pytestmark = pytest.mark.gpu
+
+
+def _edge_illum(N, M, seed):
+    rng = np.random.default_rng(seed)
+    il = oracle.illum(seed, 0.0, 2.0, N, M, independent_faces=True).reshape(M, N, 4)
+    cells = rng.permutation(N)
+    # exact ties: a float32 value plus half its ulp, times 4, on face 0 with
+    # the other faces 0 (the sum is exact)
+    f = rng.lognormal(0.0, 1.0, size=(M, 64)).astype(np.float32)
+    ulp = np.spacing(f).astype(np.float64)
+    tie = (f.astype(np.float64) + ulp / 2) * 4
+    c = cells[:64]
+    il[:, c, :] = 0.0
+    il[:, c, 0] = tie
+    # zeros, FP32-subnormal quarters (the conversion's fallback; in FP16 mode
+    # the clamped row scale), negatives, spread within a cell
+    il[:, cells[64:80], :] = 0.0
+    il[:, cells[80:96], :] = rng.uniform(1e-45, 1e-39, size=(M, 16, 4))
+    il[:, cells[96:112], :] *= -1.0
+    il[::3, cells[112:128], :] *= 1e12
+    il[1::3, cells[112:128], :] *= 1e-12
+    return il.reshape(-1)
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3", "bf16x3"])
+@pytest.mark.parametrize("M", [37, 146])
+def test_staged_rows_match_direct_rows(ctx, prec, M):
+    N = 3001
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = _edge_illum(N, M, 17)
+    ctx.init(xyz, area, fa, N)
+    ctx.set_precision(prec)
+    try:
+        S_sync = ctx.scattering(il)
+        ctx.copy_illum(il)
+        out1, out2 = np.zeros(M * N), np.zeros(M * N)
+        ctx.scattering_async(0, M // 3, STREAM_SCATTERING_1, out1)  # prepares the rows
+        ctx.scattering_async(0, M, STREAM_SCATTERING_2, out2)       # reuses them
+        ctx.wait()
+        ctx.scattering_async(M // 3, M, STREAM_SCATTERING_1, out1)  # prepares again
+        ctx.wait()
+    finally:
+        ctx.set_precision("fp64")
+    S_sync = S_sync.reshape(M, N)
+    assert np.array_equal(out2.reshape(M, N), S_sync, equal_nan=True)
+    assert np.array_equal(out1.reshape(M, N), S_sync, equal_nan=True)
+    # and the lognormal cells are the integral (the edge cells hold values a
+    # split format cannot carry to 1e-5: zeros, FP32 subnormals, 1e+-12 spreads)
+    ref = oracle.calculate_int_cpu(N, xyz, area, fa, il)
+    normal = np.ones(N, bool)
+    normal[np.random.default_rng(17).permutation(N)[:128]] = False
+    rel = np.abs(S_sync[:, normal] - ref[:, normal]) / np.abs(ref[:, normal])
+    assert float(rel.max()) <= (1e-4 if prec == "bf16x3" else 1e-5)

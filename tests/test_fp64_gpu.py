@@ -77,6 +77,50 @@ def test_async_streams_like_the_source_iteration(ctx):
     assert rel_err(ctx.host_scattering().reshape(M, N), ref) <= TOL
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp16x3"])
+def test_call_on_stream_2_waits_for_input_writes(ctx, prec):
+    """A call on scattering stream 2 sees every Illum write queued on stream 1
+    before it -- copies queued after a stream-1 call, and the Illum the FP64
+    source iteration relaxed -- while the pair of calls of the source
+    iteration overlaps (rows both cover agree bit for bit)."""
+    N, M = 20_000, 37
+    tol = TOL if prec == "fp64" else 1e-5
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il_a = oracle.illum(4, 0.0, 1.2, N, M, independent_faces=True)
+    il_b = oracle.illum(5, 0.0, 0.8, N, M, independent_faces=True)
+    ctx.init(xyz, area, fa, N)
+    ctx.set_precision(prec)
+    try:
+        out1, out2 = np.zeros(M * N), np.zeros(M * N)
+        for j in range(M):
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il_a)
+        ctx.scattering_async(0, M // 3, STREAM_SCATTERING_1, out1)
+        ctx.scattering_async(0, M, STREAM_SCATTERING_2, out2)
+        ctx.wait()
+        ref_a = oracle.calculate_int_cpu(N, xyz, area, fa, il_a)
+        assert rel_err(out2.reshape(M, N), ref_a) <= tol
+        assert np.array_equal(out1[: (M // 3) * N], out2[: (M // 3) * N])
+        # new Illum queued on stream 1 after a stream-1 call, read on stream 2
+        ctx.scattering_async(0, M, STREAM_SCATTERING_1, out1)
+        for j in range(M):
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il_b)
+        ctx.scattering_async(0, M, STREAM_SCATTERING_2, out2)
+        ctx.wait()
+        assert rel_err(out1.reshape(M, N), ref_a) <= tol
+        ref_b = oracle.calculate_int_cpu(N, xyz, area, fa, il_b)
+        assert rel_err(out2.reshape(M, N), ref_b) <= tol
+    finally:
+        ctx.set_precision("fp64")
+    # the FP64 iteration relaxes the device Illum on stream 1
+    ctx.solve_setup("fp64", oracle.uniform(2, 2, 0.1, 1.0, N), 0.9)
+    ctx.solve_step_async(True)
+    ctx.scattering_async(0, M, STREAM_SCATTERING_2, out2)
+    ctx.wait()
+    relaxed = ctx.read_illum(np.empty(M * N * 4))
+    ref_r = oracle.calculate_int_cpu(N, xyz, area, fa, relaxed)
+    assert rel_err(out2.reshape(M, N), ref_r) <= TOL
+
+
 def test_shard_of_out_directions(ctx):
     """InitDevice(start, end) shards out-directions like d_GetS_MPI_Stream."""
     N, M = 300, 50
