@@ -12,9 +12,13 @@ and distributions (the reference ships no data set).
 
 * value: cell-direction pairs per second over K timed steps with every input
   resident in HBM (inputs are larger than L2: no flush needed);
-* e2e: the same metric through the host-buffer entry point
-  rts_scattering_update (H2D of the FP64 face-layout Illum and B, integral +
-  update, D2H of the FP64 S) every step;
+* e2e: the same metric through the reference's calling sequence at the
+  bench's precision: per direction rts_send_illum_async (CudaSendIllumAsync)
+  of the FP64 face-layout Illum from pinned host memory, then the pair of
+  rts_scattering_async calls (CalculateIntScatteringAsyncMPIStream on
+  scattering streams 1 and 2, each with its D2H of S) and the waits; every
+  copy inside the timed region (e2e_host_call: the pipelined host-buffer
+  entry point rts_scattering_update);
 * roofline: the dominant kernel's algorithmic FLOP/s against the measured
   (or fallback) peak, timed with CUDA events on the library's stream;
 * cpu_baseline: the CPU restatement of the reference's CalculateIntCPU on a
@@ -704,8 +708,8 @@ def run_ours(args, rank, world, local):
                  "p99_over_isolated_p99": row.get("p99_vs_isolated_p99"),
                  "fifo_alone_p99_ms": row.get("fifo_alone_p99_ms"),
                  "fifo_alone_p99_over_isolated_p99": row.get("fifo_alone_p99_vs_isolated_p99"),
-                 "fifo_alone_p99_ms": row.get("fifo_alone_p99_ms"),
-                 "fifo_alone_p99_over_isolated_p99": row.get("fifo_alone_p99_vs_isolated_p99"),
+                 "ps_alone_p99_over_isolated_p99": row.get("ps_alone_p99_vs_isolated_p99"),
+                 "srpt_alone_p99_over_isolated_p99": row.get("srpt_alone_p99_vs_isolated_p99"),
                  "mean_queue_ms": row.get("mean_queue_ms"), "p99_queue_ms": row.get("p99_queue_ms"),
                  "throughput_cell_dir_iter_per_s": row["throughput_cell_dir_iter_per_s"],
                  "policy": sres["policy"], "window_s": args.serve_window,

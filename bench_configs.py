@@ -235,14 +235,52 @@ def fifo_latencies(arrivals, service):
     return np.array(out)
 
 
-def fifo_latencies(arrivals, service):
-    """Latencies of requests served one at a time in arrival order, each for
-    its service time (seconds)."""
-    t, out = 0.0, []
-    for a, s in zip(arrivals, service):
-        t = max(t, a) + s
-        out.append(t - a)
-    return np.array(out)
+def shared_latencies(arrivals, service, policy):
+    """Latencies of requests on one server that runs at the isolated rate of
+    whatever it serves, with preemption for free: "ps" shares it equally
+    among the requests present (processor sharing), "srpt" gives it to the
+    request with the least remaining service.  Idealised reference points
+    for the measured p99 (seconds in, seconds out)."""
+    order = np.argsort(arrivals, kind="stable")
+    arr = np.asarray(arrivals, float)[order]
+    rem = {}
+    out = np.zeros(len(arr))
+    t, i = 0.0, 0
+    while i < len(arr) or rem:
+        nxt = arr[i] if i < len(arr) else np.inf
+        if not rem:
+            t = nxt
+        else:
+            if policy == "ps":
+                n = len(rem)
+                k = min(rem, key=rem.get)
+                done_t = t + rem[k] * n
+                if done_t <= nxt:
+                    dt = done_t - t
+                    for j in rem:
+                        rem[j] -= dt / n
+                    t = done_t
+                    del rem[k]
+                    out[k] = t - arr[k]
+                    continue
+                for j in rem:
+                    rem[j] -= (nxt - t) / n
+                t = nxt
+            else:
+                k = min(rem, key=lambda j: (rem[j], j))
+                if t + rem[k] <= nxt:
+                    t += rem[k]
+                    del rem[k]
+                    out[k] = t - arr[k]
+                    continue
+                rem[k] -= nxt - t
+                t = nxt
+        while i < len(arr) and arr[i] <= t:
+            rem[i] = float(np.asarray(service, float)[order][i])
+            i += 1
+    res = np.empty(len(arr))
+    res[order] = out
+    return res
 
 
 def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2.0, precision="fp16x3",
@@ -322,16 +360,16 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
             # for its isolated time, first come first served: what queueing
             # alone costs at this load when requests gain nothing from sharing
             # the device (a reference point for the measured p99)
-            fifo = fifo_latencies([r.arrival_s for r in reqs], iso / 1e3) * 1e3
+            arrivals = [r.arrival_s for r in reqs]
+            fifo = fifo_latencies(arrivals, iso / 1e3) * 1e3
             row["fifo_alone_p99_ms"] = float(np.percentile(fifo, 99))
             row["fifo_alone_p99_vs_isolated_p99"] = row["fifo_alone_p99_ms"] / float(np.percentile(iso, 99))
-            # the same arrivals through one server that runs each request alone
-            # for its isolated time, first come first served: what queueing
-            # alone costs at this load when requests gain nothing from sharing
-            # the device (a reference point for the measured p99)
-            fifo = fifo_latencies([r.arrival_s for r in reqs], iso / 1e3) * 1e3
-            row["fifo_alone_p99_ms"] = float(np.percentile(fifo, 99))
-            row["fifo_alone_p99_vs_isolated_p99"] = row["fifo_alone_p99_ms"] / float(np.percentile(iso, 99))
+            # ... and with free preemption: processor sharing and shortest
+            # remaining service first, at the isolated rates
+            for pol in ("ps", "srpt"):
+                lat_p = shared_latencies(arrivals, iso / 1e3, pol) * 1e3
+                row[f"{pol}_alone_p99_ms"] = float(np.percentile(lat_p, 99))
+                row[f"{pol}_alone_p99_vs_isolated_p99"] = row[f"{pol}_alone_p99_ms"] / float(np.percentile(iso, 99))
         results["loads"].append(row)
     pool.close()
     ctx.set_tuning(native.TUNE_SERVE_POLICY, 1)
