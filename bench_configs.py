@@ -172,7 +172,8 @@ def config4_problems(seed=3):
 
 def config4(pkg, native, ctx, torch, steps, warmup, precision):
     probs = config4_problems()
-    tuned = {M: ctx.autotune(M, precision)[0] for M in sorted({p[1] for p in probs})}  # not timed
+    # schedule per direction count (drain period, width, order), not timed
+    tuned = {M: ctx.autotune_schedule(M, precision)[0] for M in sorted({p[1] for p in probs})}
     b = native.Batch(ctx)
     ids = []
     for (N, M, ph, g, lam, seed) in probs:
@@ -205,7 +206,8 @@ def config4(pkg, native, ctx, torch, steps, warmup, precision):
     return {"value": units * nsteps / t / 1e9, "ms_per_step": t / nsteps * 1e3, "problems": nprob, "tiles": tiles,
             "tflops_alg": flops * nsteps / t / 1e12, "graph_steps": per_graph, "gpu_launches": launches,
             "max_rel_err": max(e[0] for e in errs), "mean_rel_err": float(np.mean([e[1] for e in errs])),
-            "precision": precision, "autotuned_bn": {str(k): v for k, v in tuned.items()},
+            "precision": precision,
+            "autotuned": {str(k): {x: v[x] for x in ("flush", "bn", "order", "ms")} for k, v in tuned.items()},
             "workload": "64 problems, N log-uniform [5k,200k], M in {146,302,590}, Thomson or HG g~U[0,0.8], "
                         "lambda~U[0.2,0.95], seed 3; one grouped launch per step, CUDA-graph replay"}
 

@@ -629,17 +629,47 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value);
  * phase kernel: RTS_TUNE_FLUSH when set, else the automatic choice. */
 int rts_flush_period(const rts_ctx* ctx, int precision, int* flush);
 
-/* Autotuner of the tensor-core kernel's tile width (out-directions per
- * tile).  Times every distinct tiling of M directions (tiles of 64..256) on a
- * synthetic problem of `cells` cells (0: four waves of row tiles), keeps the
- * fastest in the context's table and reports it; problems created with
- * bn = 0 and M directions at that precision and flush then use it.  tried_bn
- * / tried_ms (capacity entries, may be NULL) receive every timing, *tried
- * their count.  Results do not depend on the tile width (same arithmetic per
- * output).  No counterpart in the reference. */
+/* Autotuner of the tensor-core kernel's schedule: drain period (K-slices
+ * per FP32 drain), tile width (out-directions per tile) and tile order.  No
+ * counterpart in the reference (its launch shape is fixed).
+ *
+ * rts_autotune_schedule times, on a synthetic Thomson problem of `cells`
+ * cells (0: four waves of 128-cell row tiles) and M Fibonacci directions at
+ * `precision`, every drain period the accuracy rule allows (FP16 / BF16: 1,
+ * and 2 where RTS_TUNE_FLUSH's automatic choice gives 2; TF32: 2), every
+ * distinct tiling of the M out-directions (tiles of 64..256) and both tile
+ * orders (0: the column tiles of a row tile in turn; 1: the row tiles of a
+ * column tile in turn).  The fastest width and order of each period enter
+ * the context's table under (M, precision, period, cell bucket), the bucket
+ * being the cell count in waves of row tiles over the SMs (below 1, 4, 16,
+ * or more).  Problems created afterwards -- batches, serving requests and the
+ * context's own calls -- take, unless their caller fixes it (desc->flush,
+ * RTS_TUNE_FLUSH), the allowed period with the shorter tuned time, and with
+ * it, unless fixed (desc->bn), that period's width, and its order, from the
+ * entry of the nearest bucket.  Width and order give bit-identical results;
+ * the period changes the rounding within the accuracy the rule guarantees.
+ * *best receives the fastest schedule; tried (capacity entries, may be NULL
+ * when capacity is 0) every timing, *n_tried their count. */
+typedef struct rts_tune_choice {
+    int64_t M;
+    int precision;
+    int flush;   /* K-slices per drain */
+    int bn;      /* out-directions per tile */
+    int order;   /* 0: column tiles of a row tile in turn; 1: row tiles of a column tile */
+    int bucket;  /* cell bucket of the timing problem */
+    double ms;   /* one relaxed step of the timing problem */
+} rts_tune_choice;
+int rts_autotune_schedule(rts_ctx* ctx, int64_t M, int precision, int64_t cells, rts_tune_choice* best,
+                          rts_tune_choice* tried, int capacity, int* n_tried);
+/* The width-only search at one drain period (flush 0: the automatic one),
+ * tile order 0; the fastest width enters the table as above.  tried_bn /
+ * tried_ms (capacity entries, may be NULL) receive every timing, *tried their
+ * count. */
 int rts_autotune(rts_ctx* ctx, int64_t M, int precision, int flush, int64_t cells, int* best_bn, double* best_ms,
                  int* tried_bn, double* tried_ms, int capacity, int* tried);
-/* The table as text ("M precision flush bn ms" per line), and back. */
+/* The table as text ("M precision flush cell_bucket bn order ms" per line),
+ * and back (tables of "M precision flush bn ms" lines load as entries for
+ * every bucket, order 0). */
 int rts_autotune_save(rts_ctx* ctx, const char* path);
 int rts_autotune_load(rts_ctx* ctx, const char* path);
 

@@ -120,6 +120,7 @@ _SIGNATURES = {
     "rts_flush_period": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "rts_autotune": (C.c_int, [_vp, _i64, C.c_int, C.c_int, _i64, C.POINTER(C.c_int), _dp, C.POINTER(C.c_int), _dp,
                                C.c_int, C.POINTER(C.c_int)]),
+    "rts_autotune_schedule": (C.c_int, [_vp, _i64, C.c_int, _i64, _vp, _vp, C.c_int, C.POINTER(C.c_int)]),
     "rts_autotune_save": (C.c_int, [_vp, C.c_char_p]),
     "rts_autotune_load": (C.c_int, [_vp, C.c_char_p]),
     "rts_stream_handle": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
@@ -259,6 +260,15 @@ def synth_uniform(seed: int, stream: int, lo: float, hi: float, n: int, i0: int 
     if rc != OK:
         raise RtsError(rc, "rts_synth_uniform")
     return out
+
+class TuneChoice(C.Structure):
+    """rts_tune_choice"""
+    _fields_ = [("M", C.c_int64), ("precision", C.c_int), ("flush", C.c_int), ("bn", C.c_int), ("order", C.c_int),
+                ("bucket", C.c_int), ("ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 
 class ProblemDesc(C.Structure):
     """rts_problem_desc"""
@@ -608,6 +618,18 @@ class Context:
         self._check(self.lib.rts_autotune(self.h, int(M), prec, int(flush), int(cells), C.byref(best), C.byref(best_ms),
                                           bns, mss, 16, C.byref(tried)), "rts_autotune")
         return best.value, best_ms.value, {bns[i]: mss[i] for i in range(min(tried.value, 16))}
+
+    def autotune_schedule(self, M: int, precision="fp16x3", cells: int = 0):
+        """Fastest (drain period, tile width, tile order) for M directions;
+        returns (best, tried), each schedule a dict."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        cap = 64
+        best = TuneChoice()
+        tried = (TuneChoice * cap)()
+        n = C.c_int()
+        self._check(self.lib.rts_autotune_schedule(self.h, int(M), prec, int(cells), C.byref(best), tried, cap,
+                                                   C.byref(n)), "rts_autotune_schedule")
+        return best.as_dict(), [tried[i].as_dict() for i in range(min(n.value, cap))]
 
     def autotune_save(self, path):
         self._check(self.lib.rts_autotune_save(self.h, str(path).encode()), "rts_autotune_save")

@@ -105,7 +105,10 @@ int rts_batch_add_on(rts_batch* batch, const rts_problem_desc* d, const float* i
     if (rc != RTS_OK) return rc;
 
     GProb* p = nullptr;
-    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g, d->precision);
+    const int flush = d->flush > 0 ? d->flush
+                                   : rts_tuned_flush(ctx, M, d->precision, N * G,
+                                                     rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M,
+                                                                    d->phase, d->g, d->precision));
     rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), flush, d->bn, true, &p, st);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);
@@ -292,7 +295,10 @@ extern "C" int rts_batch_add_synthetic(rts_batch* batch, const rts_problem_desc*
     rc = rts_launch_weights_raw(ctx, d_xyz, d_area, (int)M, 0, (int)M, full_area, d->phase, d->g, W, st);
     if (rc != RTS_OK) return rc;
     GProb* p = nullptr;
-    const int flush = d->flush > 0 ? d->flush : rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M, d->phase, d->g, d->precision);
+    const int flush = d->flush > 0 ? d->flush
+                                   : rts_tuned_flush(ctx, M, d->precision, N * G,
+                                                     rts_auto_flush(xyz.data(), area.data(), M, full_area, 0, M,
+                                                                    d->phase, d->g, d->precision));
     rc = rts_group_new_problem(batch, N, M, M, G, W, (int)M, rts_split_mode(d->precision), flush, d->bn, true, &p);
     if (rc != RTS_OK) return rc;
     std::vector<float> lam((size_t)G);

@@ -109,7 +109,7 @@ void free_prob(rts_ctx* ctx, GProb* p, cudaStream_t st)
     rts_pfree(ctx, p->B, (size_t)(p->rows * 4), st);
     rts_pfree(ctx, p->lam, (size_t)(p->groups * 4), st);
     rts_pfree(ctx, p->S32, (size_t)(p->rows * p->Mout * 4), st);
-    rts_pfree(ctx, p->vrow, (size_t)((p->kpad + 1) * 4), st);
+    rts_pfree(ctx, p->vrow, (size_t)((p->kpad + 4) * 4), st);
     rts_pfree(ctx, p->part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), st);
     rts_pfree(ctx, p->delta, (size_t)(p->rows_pad * 4), st);
     rts_pfree(ctx, p->ex, (size_t)(p->rows_pad * 8), st);
@@ -154,7 +154,7 @@ float rts_group_bias(const rts_ctx* ctx, int, int)
 
 int64_t rts_group_energy_bytes(int64_t kpad, int64_t rows_pad, int n_tiles)
 {
-    return (kpad + 1) * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 12;
+    return (kpad + 4) * 4 + (int64_t)n_tiles * 4 * rows_pad * 16 + rows_pad * 12;
 }
 
 // Tile geometry of a problem: out-direction tiles of at most G_BN (256), balanced.
@@ -180,7 +180,8 @@ int64_t rts_group_footprint(int64_t N, int64_t M, int64_t groups, bool iterative
     int bn, nt;
     int64_t kpad, mpad, rows_pad, mt;
     const int64_t rows = N * groups;
-    rts_group_geometry(M, M, rows, 0, &bn, &nt, &kpad, &mpad, &rows_pad, &mt);
+    // an iteration's tiles also cover the correction's extra output column
+    rts_group_geometry(M, iterative ? M + 1 : M, rows, 0, &bn, &nt, &kpad, &mpad, &rows_pad, &mt);
     const int64_t units = (mode == 2 ? 4 : 2) * kpad;
     int64_t bytes = mpad * units * 2 + 2 * mpad * 4 + 2 * rows_pad * 4 + rows * 4 + groups * 4;
     bytes += (iterative ? 2 : 1) * rows_pad * units * 2;
@@ -207,9 +208,19 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     p->fp16 = fp16;
     p->mode = mode;
     p->flush = std::min(std::max(flush, 1), G_MAX_FLUSH);
-    if (bn_override <= 0 && Mout == Min) bn_override = rts_tuned_bn(ctx, Min, mode, p->flush);  // 0 if not tuned
-    rts_group_geometry(Min, Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad, &p->rows_pad,
-                       &p->m_tiles);
+    {  // the autotuner's width (problems of all M out-directions without a width of their own) and tile order
+        int tbn = 0, torder = 0;
+        if (rts_tuned_tile(ctx, Min, mode, p->flush, p->rows, &tbn, &torder)) {
+            if (bn_override <= 0 && Mout == Min) bn_override = tbn;
+            p->order = torder;
+        }
+    }
+    // the conservation correction of relaxed steps (iterations over all M
+    // out-directions) takes one extra output column, index Mout: its W^T row
+    // gives sum_j d_j (W^T x)_j (rts_pp_w_stats).  Every tiling has it.
+    const bool energy = iterative && Mout == Min;
+    rts_group_geometry(Min, energy ? Mout + 1 : Mout, p->rows, bn_override, &p->bn, &p->n_tiles, &p->kpad, &p->mpad,
+                       &p->rows_pad, &p->m_tiles);
     int rc;
     void* q;
     if (!st) st = ctx->streams[RTS_STREAM_SCATTERING_1];
@@ -237,12 +248,11 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     }
     GP_ALLOC(B, (size_t)(p->rows * 4), "source B");
     GP_ALLOC(lam, (size_t)(p->groups * 4), "albedo");
-    const bool energy = iterative && Mout == Min;
     if (iterative) {
         GP_ALLOC(S32, (size_t)(p->rows * p->Mout * 4), "FP32 scattering");
     }
     if (energy) {
-        GP_ALLOC(vrow, (size_t)((p->kpad + 1) * 4), "W row sums");
+        GP_ALLOC(vrow, (size_t)((p->kpad + 4) * 4), "W row sums");
         GP_ALLOC(part, (size_t)(p->n_tiles * 4 * p->rows_pad * 16), "energy partial sums");
         GP_ALLOC(delta, (size_t)(p->rows_pad * 4), "energy corrections");
         GP_ALLOC(ex, (size_t)(p->rows_pad * 8), "conserved sums");
@@ -251,8 +261,7 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (!ext_a) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[0], 0, abytes, st));
     if (p->a[1]) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->a[1], 0, abytes, st));
     if (p->S32) RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->S32, 0, (size_t)(p->rows * p->Mout * 4), st));
-    rc = rts_pp_split_w(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, (int)p->mpad, mode, p->wc, p->cs, st);
-    if (rc == RTS_OK && p->vrow) rc = rts_pp_row_sums(ctx, W_dev, (int)Min, (int)Mout, ldw, (int)p->kpad, p->vrow, st);
+    rc = rts_group_set_w(ctx, p, W_dev, ldw, st);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[2], p->wc, p->mpad, p->units, p->bn);
     if (rc == RTS_OK) rc = make_map(ctx, p->maps[0], p->a[0], p->rows_pad, p->units, G_BM);
     if (rc == RTS_OK && p->a[1]) rc = make_map(ctx, p->maps[1], p->a[1], p->rows_pad, p->units, G_BM);
@@ -266,6 +275,25 @@ int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, in
     if (!p->a[1]) memcpy(p->rmaps[1], p->rmaps[0], 128);
     *out = p;
     return RTS_OK;
+}
+
+int rts_group_set_w(rts_ctx* ctx, GProb* p, const double* W_dev, int ldw, cudaStream_t st)
+{
+    const int Min = (int)p->M, Mout = (int)p->Mout;
+    if (!p->vrow)
+        return rts_pp_split_w(ctx, W_dev, Min, Mout, ldw, (int)p->kpad, (int)p->mpad, p->mode, p->wc, p->cs, st);
+    // the correction's statistics and extra row (FP64 scratch, stream-ordered)
+    void* scratch = nullptr;
+    const size_t sbytes = (size_t)Min * 2 * sizeof(double);
+    int rc = rts_pmalloc(ctx, &scratch, sbytes, "W statistics scratch", st);
+    if (rc != RTS_OK) return rc;
+    double* v64 = static_cast<double*>(scratch);
+    double* u = v64 + Min;
+    rc = rts_pp_w_stats(ctx, W_dev, Min, Mout, ldw, (int)p->kpad, p->vrow, v64, u, st);
+    if (rc == RTS_OK)
+        rc = rts_pp_split_w(ctx, W_dev, Min, Mout, ldw, (int)p->kpad, (int)p->mpad, p->mode, p->wc, p->cs, st, u);
+    rts_pfree(ctx, scratch, sbytes, st);
+    return rc;
 }
 
 int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st)
@@ -352,6 +380,7 @@ static void fill_entry(rts_batch* b, GProb* p, int relax, size_t i, int64_t& til
     g.kblocks = (int)(p->kpad / (p->mode == 2 ? 16 : 32));
     g.bn = p->bn;
     g.flush = p->flush;
+    g.order = p->order;
     g.groups = (int)p->groups;
     g.idesc = rts_ptx::idesc_split(p->mode, G_BM, p->bn);
     g.bias = rts_group_bias(ctx, p->mode, p->flush);

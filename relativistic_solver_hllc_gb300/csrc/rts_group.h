@@ -17,6 +17,7 @@ struct GProb {
     int64_t id = 0;
     int64_t N = 0, M = 0, Mout = 0, groups = 1, rows = 0, rows_pad = 0, kpad = 0, mpad = 0;  // M: in-directions
     int bn = 0, n_tiles = 0, flush = 1;
+    int order = 0;           // tile order of the kernel (GroupProblem::order)
     int64_t m_tiles = 0;
     bool fp16 = true;        // FP16 split with row / column scales (mode 1)
     int mode = 1;            // split mode: 0 BF16, 1 FP16, 2 TF32
@@ -36,7 +37,7 @@ struct GProb {
     int slot = -1;           // index of the problem's residual in the last launched table
     size_t bytes = 0;
     // energy-conservation correction of relaxed steps (iterative problems)
-    float* vrow = nullptr;   // [kpad + 1] v_j = sum_k W[j][k]; [kpad]: the quantum scale of the partial sums
+    float* vrow = nullptr;   // [kpad + 4] v_j = sum_k W[j][k]; then the quantum scale, c, D, 1/c (rts_pp_w_stats)
     void* part = nullptr;    // [n_tiles * 4][rows_pad] int4 per-slot partial sums of a step (fixed point)
     float* delta = nullptr;  // [rows_pad] per-row correction of the next step
     double* ex = nullptr;    // [rows_pad] sum_j v_j x_j of the current input (fixed-point quanta)
@@ -55,6 +56,9 @@ void rts_group_batch_free(rts_batch* b);
 int rts_group_new_problem(rts_batch* b, int64_t N, int64_t Min, int64_t Mout, int64_t groups, const double* W_dev, int ldw,
                           int mode, int flush, int bn_override, bool iterative, GProb** out, cudaStream_t st = nullptr,
                           uint16_t* ext_a = nullptr, float* ext_rs = nullptr);
+// W (and, for problems with the correction, its statistics and extra row)
+// into the problem's split W^T rows, on st.
+int rts_group_set_w(rts_ctx* ctx, GProb* p, const double* W_dev, int ldw, cudaStream_t st);
 int rts_group_attach(rts_batch* b, GProb* p, int64_t* id);
 GProb* rts_group_find(rts_batch* b, int64_t id, size_t* index);
 int rts_group_remove(rts_batch* b, int64_t id);

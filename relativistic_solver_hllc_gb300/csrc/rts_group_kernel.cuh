@@ -98,6 +98,7 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     int64_t tile_off;     // the problem's own first tile in this launch (a step may span launches)
     int m_tiles, n_tiles;
     int Mout, kpad, kblocks, bn, flush, groups;
+    int order;            // tile order: 0 the column tiles of a row tile in turn, 1 the row tiles of a column tile
     uint32_t idesc;
     float bias;           // relative correction of the truncation bias of the sums
     int fp16;
@@ -116,7 +117,9 @@ struct GroupProblem {  // aligned as its CUtensorMap members
     uint16_t* a[2];       // [rows_pad][2*kpad] interleaved split rows
     unsigned long long* resid;  // residual bits of this problem's step
     // energy-conservation correction of relaxed steps (null: none)
-    const float* vrow;    // [kpad + 1] v_j = sum_k W[j][k], 0 past M; vrow[kpad] = q0 (below)
+    const float* vrow;    // [kpad + 4] v_j = sum_k W[j][k], 0 past M; vrow[kpad] = q0 (below), then c, D, 1/c:
+                          // c the mean of the v_j, D = sum_j (v_j - c); output column Mout holds
+                          // sum_j (v_j - c) raw_j
     int4* part;           // [n_tiles * 4][rows_pad] per-slot partials in quanta (high, low parts):
                           // sum_j v_j rs S_j, then sum_k raw_k
     double* ex;           // [rows_pad] sum_j v_j x_j of the current input, in quanta
@@ -161,6 +164,18 @@ __device__ __forceinline__ int find_problem(const GroupProblem* probs, int nprob
             hi = mid - 1;
     }
     return lo;
+}
+
+// Row and column tile of a problem's tile lt (0 <= lt < m_tiles * n_tiles).
+__device__ __forceinline__ void tile_coords(const GroupProblem& P, int64_t lt, int& m_tile, int& n_tile)
+{
+    if (P.order) {
+        m_tile = (int)(lt % P.m_tiles);
+        n_tile = (int)(lt / P.m_tiles);
+    } else {
+        m_tile = (int)(lt / P.n_tiles);
+        n_tile = (int)(lt % P.n_tiles);
+    }
 }
 
 // Relaxation of 8 columns of one split row in place (shared memory):
@@ -251,8 +266,10 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
                 const GroupProblem& P = probs[find_problem(probs, nprob, t)];
                 const int64_t lt = t - P.tile_begin + P.tile_off;
-                const int n_tiles = P.n_tiles, nkb = P.kblocks, bn = P.bn;
-                const int m0 = (int)(lt / n_tiles) * G_BM, n0 = (int)(lt % n_tiles) * bn;
+                const int nkb = P.kblocks, bn = P.bn;
+                int m_tile, n_tile;
+                tile_coords(P, lt, m_tile, n_tile);
+                const int m0 = m_tile * G_BM, n0 = n_tile * bn;
                 const void* mapA = &P.mapA[P.cur];
                 const void* mapW = &P.mapW;
                 const uint32_t tx = (uint32_t)(G_A_BYTES + bn * 128);
@@ -359,7 +376,8 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const int sw = P.sw;                         // columns per slice (multiple of 16, <= 64)
             const int ncols = min(sw, bn - sw * cs);  // columns of this warp (multiple of 16; <= 0: none)
             const int64_t lt = t - P.tile_begin + P.tile_off;
-            const int m_tile = (int)(lt / P.n_tiles), n_tile = (int)(lt % P.n_tiles);
+            int m_tile, n_tile;
+            tile_coords(P, lt, m_tile, n_tile);
             float run[64];
 #pragma unroll
             for (int j = 0; j < 64; ++j) run[j] = 0.0f;
@@ -458,25 +476,17 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             const float hrsc = 0.5f * ((fp16 && in_row) ? P.rs[r] : 1.0f);
             const bool want_rel = kEnergy || (relax && P.S64 == nullptr);  // relax implies Mout == M <= kpad
             // energy-conservation correction (relaxed steps): this cell's delta
-            // from the previous step; the partial sums of this one.  `ewarp`
-            // is uniform over the warp (the shuffles of v_j need every lane).
+            // from the previous step; the partial sums of this one.
             const bool ewarp = kEnergy && want_rel && P.part != nullptr;
             const float qrow = (ewarp && in_row) ? energy_scale(P, r, fp16) : 0.0f;
             const bool cons = qrow > 0.0f;
             const float bias = P.bias + (cons ? P.delta[r] : 0.0f);
-            // the sum of v_j S_j in the units of x (scaled by rs in FP16 mode)
-            const float qv = fp16 ? qrow * 2.0f * hrsc : qrow;
-            int xh = 0, xl = 0, th = 0, tl = 0;  // fixed-point partial sums (sum_j v_j rs S_j, sum_k raw_k)
-            float vp0 = 0.0f, vp1 = 0.0f;        // v_j of this warp's columns kbase + 2 lane, + 1
+            // the partial sums: sum_k raw_k in fixed point, and the raw value
+            // of the extra column Mout (sum_j (v_j - c) raw_j) where this warp
+            // holds it; group_energy_kernel derives sum_j v_j S_j from them
+            int th = 0, tl = 0;
+            float raw_e = 0.0f;
             const int kbase = n_tile * bn + sw * cs;
-            if (ewarp) {
-                const int c0 = kbase + 2 * lane;
-                if (2 * lane < ncols && c0 < P.kpad) {
-                    const float2 v2 = __ldg(reinterpret_cast<const float2*>(P.vrow + c0));
-                    vp0 = v2.x;
-                    vp1 = v2.y;
-                }
-            }
             float* __restrict__ S = P.S32 ? P.S32 + grp * (int64_t)Mout * ld + cc : nullptr;
             // (the energy instantiation runs relaxed source iterations, whose output is S32)
             double* __restrict__ S64 = (!kEnergy && P.S64) ? P.S64 + grp * (int64_t)Mout * ld + cc : nullptr;
@@ -556,24 +566,16 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
                     float v[8];
                     tmem_ld8(last_acc + (uint32_t)e0, v);
                     float snew[8];
-                    float eb = 0.0f;  // these 8 columns' raw integrals, in column order
+                    float eb = 0.0f;  // these columns' raw integrals, in column order
     #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const float raw = v[j] * cin[j];  // cin is a power of two: exact
-                        if (kEnergy && j < nk) eb += raw;
                         snew[j] = fmaf(fmaf(raw, bias, raw), lr, bterm);
+                        if (kEnergy && j < nk) eb += raw;
+                        if (kEnergy && j == nk) raw_e = raw;  // column Mout (one block of one warp)
                     }
                     // blocks of 8 columns start at multiples of 8 of the out-directions
                     if (kEnergy && cons && live_k) fixed_add(eb * qrow, th, tl);
-                    if (kEnergy && ewarp) {  // sum_j v_j S_j of these columns (every lane shuffles)
-                        float ev = 0.0f;
-    #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const float vj = __shfl_sync(0xffffffffu, (j & 1) ? vp1 : vp0, (e0 + j) >> 1);
-                            if (j < nk) ev = fmaf(vj, snew[j], ev);
-                        }
-                        if (cons && live_k) fixed_add(ev * qv, xh, xl);
-                    }
                     if (live_k) {
                         if (S64) {
                             double* dp = S64 + (int64_t)k0 * ld;
@@ -647,7 +649,7 @@ group_kernel(const GroupProblem* __restrict__ probs, int nprob, int64_t total_ti
             release_last();
             if (kEnergy && ewarp && in_row && ok) {  // this slot's partial sums (zero: no correction)
                 const int64_t slot = (int64_t)n_tile * 4 + cs;
-                P.part[slot * (P.m_tiles * (int64_t)G_BM) + r] = make_int4(xh, xl, th, tl);
+                P.part[slot * (P.m_tiles * (int64_t)G_BM) + r] = make_int4(cons ? __float_as_int(raw_e) : 0, 0, th, tl);
             }
             if (overflow) atomicOr(flag, FLAG_SCALE_OVERFLOW);
             if (residual) {
@@ -679,16 +681,31 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
     const int64_t ld = P.m_tiles * (int64_t)G_BM;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.rows;
          r += (int64_t)gridDim.x * blockDim.x) {
-        long long ev = 0, et = 0;  // exact: in units of 2^-22 of the row's quantum
+        long long et = 0;  // exact: in units of 2^-22 of the row's quantum
+        float raw_e = 0.0f;  // held by one slot, zero in the others
         for (int nt = 0; nt < P.n_tiles; ++nt)
             for (int cs = 0; cs < 4; ++cs) {
                 if (P.sw * cs >= P.bn) continue;  // a column slice without columns
                 const int4 v = P.part[((int64_t)nt * 4 + cs) * ld + r];
-                ev += ((long long)v.x << 22) + v.y;
+                raw_e += __int_as_float(v.x);
                 et += ((long long)v.z << 22) + v.w;
             }
         const double q22 = 1.0 / 4194304.0;  // the slots' units, in quanta
         const double ex = P.ex[r];           // sum_j v_j x_j of this step's input, in quanta
+        const bool fp16 = P.fp16 != 0;
+        const float qrow = energy_scale(P, r, fp16);
+        // the step's S_j = (1 + b) lr raw_j + bterm (lr = lam / rs, rs = 1
+        // for the unscaled formats), so with v_j = c + d_j
+        //   rs sum_j v_j S_j = (1 + b) lam (c sum_j raw_j + sum_j d_j raw_j) + rs bterm sum_j v_j,
+        // the raw sums in the units the epilogue sees (scaled by rs)
+        const float d_old = P.delta[r];
+        const double b1 = 1.0 + (double)(P.bias + (qrow > 0.0f ? d_old : 0.0f));
+        const int64_t grp = r / P.N;
+        const double lam = (double)P.lam[grp];
+        const double bterm = P.B ? (1.0 - lam) * (double)P.B[r] : 0.0;
+        const double rs = fp16 ? (double)P.rs[r] : 1.0;
+        const double c = (double)P.vrow[P.kpad + 1], V = c * P.Mout + (double)P.vrow[P.kpad + 2];
+        const double ev = b1 * lam * (c * ((double)et * q22) + (double)raw_e * qrow) + rs * bterm * V * qrow;
         float d = 0.0f;
         if (ex > 0.0 && et > 0) {
             const double g = ex / ((double)et * q22) - 1.0;
@@ -696,7 +713,7 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
         }
         P.delta[r] = d;
         // the next input is x / 2 + rs S / 2
-        P.ex[r] = 0.5 * ex + 0.5 * ((double)ev * q22);
+        P.ex[r] = qrow > 0.0f ? 0.5 * ex + 0.5 * ev : 0.0;
     }
 }
 

@@ -44,9 +44,11 @@ constexpr int64_t RTS_RESID_CAP = 4096;
 struct rts_batch;
 constexpr int RTS_HOST_CHUNKS = 16;  // cell ranges of a pipelined host-buffer call
 
-struct rts_tune_entry {  // autotuned tile width of the tensor-core kernel
+struct rts_tune_entry {  // autotuned schedule of the tensor-core kernel
     int64_t M = 0;
-    int precision = 0, flush = 1, bn = 0;
+    int precision = 0, flush = 1;
+    int bucket = -1;  // cell-count bucket (rts_cells_bucket); -1: any (tables without buckets)
+    int bn = 0, order = 0;
     double ms = 0.0;
 };
 
@@ -256,8 +258,9 @@ inline void rts_inputs_changed(rts_ctx* ctx)
 }
 
 inline int rts_split_mode(int precision) { return precision == RTS_PREC_FP16X3 ? 1 : precision == RTS_PREC_TF32X3 ? 2 : 0; }
+// extra (may be null): [Min] values of W^T row Mout (which must be < mpad)
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
-                   uint16_t* Wc, float* cs, cudaStream_t st);
+                   uint16_t* Wc, float* cs, cudaStream_t st, const double* extra = nullptr);
 // rs: per-row power-of-two scales putting 2 max(|Ibar|, |B|) into [2^13, 2^14)
 // (and their inverses), computed in FP16 mode -- where the split applies them --
 // and, with `bound`, in the other modes too, where they only bound the rows.
@@ -276,10 +279,14 @@ int rts_pp_rows_from_faces_staged(rts_ctx* ctx, const double* illum, int64_t N, 
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
-// v[j] = sum_{k < Mout} W[j][k] in FP64, stored as FP32, for j < Min; 0 up to
-// kpad; v[kpad] = 2^(7 - ceil(log2 sum_jk |W_jk|)) (the scale of the relaxed
-// steps' energy partial sums).
-int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st);
+// Statistics of W (Mout == Min) for the conservation correction of relaxed
+// steps, v [kpad + 4] FP32: v[j] = sum_k W[j][k] (FP64 sums) for j < Min, 0
+// up to kpad; v[kpad] = 2^(7 - ceil(log2 sum_jk |W_jk|)) (the scale of the
+// partial sums); v[kpad+1] c = the FP32 mean of the v_j; v[kpad+2] D = sum_j
+// (v_j - c); v[kpad+3] = 1 / c.  u [Min] FP64: u_i = sum_j W[i][j] (v_j - c),
+// the extra W^T row.  v64 [Min] FP64 scratch.
+int rts_pp_w_stats(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, double* v64,
+                   double* u, cudaStream_t st);
 int rts_pp_f64_to_f32(rts_ctx* ctx, const double* s, float* d, int64_t n, cudaStream_t st);
 
 // Drain period (K-slices per FP32 drain) of the tensor-core path for a
@@ -293,7 +300,16 @@ int rts_auto_flush(const double* xyz, const double* area, int64_t M, double full
 int rts_ctx_flush(const rts_ctx* ctx, int precision);
 
 // Tensor-core path (rts_split.cu).
-int rts_tuned_bn(const rts_ctx* ctx, int64_t M, int mode, int flush);
+// Autotuner tables (rts_tune.cpp).  Bucket of a problem's rows (cells x
+// groups) in waves of 128-row tiles over the SMs: 0 below one wave, 1 below
+// 4, 2 below 16, 3 from 16.
+int rts_cells_bucket(const rts_ctx* ctx, int64_t rows);
+// The drain period for a problem whose automatic period is `cap`: the tuned
+// period with the shortest time among those allowed (1..cap for FP16 / BF16,
+// cap itself for TF32), else cap.
+int rts_tuned_flush(const rts_ctx* ctx, int64_t M, int precision, int64_t rows, int cap);
+// The tuned tile width and order at that drain period; false if none.
+bool rts_tuned_tile(const rts_ctx* ctx, int64_t M, int mode, int flush, int64_t rows, int* bn, int* order);
 int rts_split_setup(rts_ctx* ctx, int precision);
 int rts_split_step(rts_ctx* ctx, bool relax, cudaStream_t st);
 // One evaluation from the device Illum (faces) into the FP64 device S, with

@@ -37,15 +37,33 @@ __device__ __forceinline__ float pow2_scale(double m)
     return ldexpf(1.0f, max(-126, min(127, 13 - ilogb(m))));
 }
 
-// W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad].
-// v[j] = sum_k W[j][k] (FP64, k in order) for j < Min, 0 up to kpad, and in
-// v[kpad] the scale of the energy partial sums, 2^(7 - ceil(log2 sum_jk
-// |W_jk|)).  One block.
-__global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict__ W, int Min, int Mout, int ldw,
-                                                       int kpad, float* __restrict__ v)
+// Block sum of one double per thread (blockDim.x a multiple of 32); every
+// thread receives the total.
+__device__ double block_sum(double x, double* red)
 {
-    __shared__ double tot[32];
-    double a = 0.0;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();  // red may still be read from a previous call
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    return t;
+}
+
+// Statistics of W [Min][ldw] FP64 (column k = out-direction, Mout == Min) for
+// the conservation correction of relaxed steps, in v [kpad + 4] (FP32):
+//   v[j] = sum_k W[j][k] (FP64 sums, k in order) for j < Min, 0 up to kpad;
+//   v[kpad] the scale of the partial sums, 2^(7 - ceil(log2 sum_jk |W_jk|));
+//   v[kpad+1] c, the FP32 value of the mean of the v_j; v[kpad+2] D, the sum
+//   of d_j = v_j - c; v[kpad+3] 1 / c;
+// and u [Min] FP64, u_i = sum_j W[i][j] d_j: the extra row of W^T whose
+// output is sum_j d_j (W^T x)_j.  v64 [Min] FP64 scratch.  One block.
+__global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict__ W, int Min, int Mout, int ldw,
+                                                       int kpad, float* __restrict__ v, double* __restrict__ v64,
+                                                       double* __restrict__ u)
+{
+    __shared__ double red[32];
+    double a = 0.0, sv = 0.0;
     for (int j = threadIdx.x; j < kpad; j += blockDim.x) {
         double s = 0.0;
         if (j < Min)
@@ -55,31 +73,51 @@ __global__ void __launch_bounds__(1024) w_stats_kernel(const double* __restrict_
                 a += fabs(w);
             }
         v[j] = (float)s;
+        if (j < Min) {
+            v64[j] = s;
+            sv += s;
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if ((threadIdx.x & 31) == 0) tot[threadIdx.x >> 5] = a;
-    __syncthreads();
+    a = block_sum(a, red);
+    sv = block_sum(sv, red);  // (its barriers also publish v64 to the block)
+    const float c = Min > 0 ? (float)(sv / Min) : 0.0f;
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tot[w];
         float q = 0.0f;
-        if (t > 0.0 && isfinite(t)) {
-            const int e = 7 - (int)ceil(log2(t));
+        if (a > 0.0 && isfinite(a)) {
+            const int e = 7 - (int)ceil(log2(a));
             if (e > -126 && e < 127) q = ldexpf(1.0f, e);
         }
         v[kpad] = q;
+        v[kpad + 1] = c;
+        v[kpad + 3] = c != 0.0f ? 1.0f / c : 0.0f;
     }
+    double ds = 0.0;
+    for (int i = threadIdx.x; i < Min; i += blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < Mout; ++j) s += W[(int64_t)i * ldw + j] * (v64[j] - (double)c);
+        u[i] = s;
+        ds += v64[i] - (double)c;
+    }
+    ds = block_sum(ds, red);
+    if (threadIdx.x == 0) v[kpad + 2] = (float)ds;
 }
 
+// W [Min][ldw] FP64 (column k = out-direction) -> Wc [mpad][2*kpad] split
+// W^T rows; with `extra`, row Mout holds extra [Min] (the correction's row).
 __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, int ldw, int kpad, int mpad,
-                               int mode, uint16_t* __restrict__ Wc, float* __restrict__ cs)
+                               int mode, uint16_t* __restrict__ Wc, float* __restrict__ cs,
+                               const double* __restrict__ extra)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= mpad) return;
     const int units = (mode == 2 ? 4 : 2) * kpad;
     uint16_t* row = Wc + (int64_t)k * units;
     float* cs_inv = cs + mpad;
-    if (k >= Mout) {
+    // element j of this row: column k of W, or the extra row
+    const bool ex = extra && k == Mout;
+    const double* col = ex ? extra : W + k;
+    const int64_t step = ex ? 1 : ldw;
+    if (k >= Mout && !ex) {
         for (int j = 0; j < units; ++j) row[j] = 0;
         cs[k] = 1.0f;
         cs_inv[k] = 1.0f;
@@ -89,7 +127,7 @@ __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, 
         float* rowf = reinterpret_cast<float*>(row);
         for (int j = 0; j < kpad; ++j) {
             float hi = 0.0f, lo = 0.0f;
-            if (j < Min) split_tf32((float)W[(int64_t)j * ldw + k], hi, lo);
+            if (j < Min) split_tf32((float)col[j * step], hi, lo);
             rowf[ilv_hi_tf32(j)] = hi;
             rowf[ilv_hi_tf32(j) + 16] = lo;
         }
@@ -101,12 +139,12 @@ __global__ void split_w_kernel(const double* __restrict__ W, int Min, int Mout, 
     float s = 1.0f;
     if (fp16) {
         double m = 0.0;
-        for (int j = 0; j < Min; ++j) m = fmax(m, fabs(W[(int64_t)j * ldw + k]));
+        for (int j = 0; j < Min; ++j) m = fmax(m, fabs(col[j * step]));
         s = pow2_scale(m);
     }
     for (int j = 0; j < kpad; ++j) {
         uint16_t hi = 0, lo = 0;
-        if (j < Min) split_any(fp16 != 0, (float)(W[(int64_t)j * ldw + k] * (double)s), hi, lo);
+        if (j < Min) split_any(fp16 != 0, (float)(col[j * step] * (double)s), hi, lo);
         row[ilv_hi(j)] = hi;
         row[ilv_hi(j) + 32] = lo;
     }
@@ -394,18 +432,19 @@ int blocks_for(rts_ctx* ctx, int64_t n, int threads)
 
 }  // namespace
 
-int rts_pp_row_sums(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, cudaStream_t st)
+int rts_pp_w_stats(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, float* v, double* v64,
+                   double* u, cudaStream_t st)
 {
-    w_stats_kernel<<<1, 1024, 0, st>>>(W, Min, Mout, ldw, kpad, v);
+    w_stats_kernel<<<1, 1024, 0, st>>>(W, Min, Mout, ldw, kpad, v, v64, u);
     RTS_CHECK_LAUNCH(ctx, "w_stats_kernel");
     ctx->launches++;
     return RTS_OK;
 }
 
 int rts_pp_split_w(rts_ctx* ctx, const double* W, int Min, int Mout, int ldw, int kpad, int mpad, int mode,
-                   uint16_t* Wc, float* cs, cudaStream_t st)
+                   uint16_t* Wc, float* cs, cudaStream_t st, const double* extra)
 {
-    split_w_kernel<<<(mpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, mpad, mode, Wc, cs);
+    split_w_kernel<<<(mpad + 127) / 128, 128, 0, st>>>(W, Min, Mout, ldw, kpad, mpad, mode, Wc, cs, extra);
     RTS_CHECK_LAUNCH(ctx, "split_w_kernel");
     ctx->launches++;
     return RTS_OK;

@@ -16,8 +16,9 @@
 int rts_ctx_flush(const rts_ctx* ctx, int precision)
 {
     if (ctx->split_flush > 0) return ctx->split_flush;
-    return rts_auto_flush(ctx->h_xyz.data(), ctx->h_area.data(), ctx->M, ctx->full_area, ctx->out_start, ctx->out_end,
-                          ctx->phase, ctx->phase_g, precision);
+    const int cap = rts_auto_flush(ctx->h_xyz.data(), ctx->h_area.data(), ctx->M, ctx->full_area, ctx->out_start,
+                                   ctx->out_end, ctx->phase, ctx->phase_g, precision);
+    return rts_tuned_flush(ctx, ctx->M, precision, ctx->N, cap);
 }
 
 namespace {
@@ -48,9 +49,9 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
         rc = rts_group_attach(*pb, p, id);
         if (rc != RTS_OK) return rc;
     } else {
-        // W may have changed (phase / custom weights): split it again
-        int rc = rts_pp_split_w(ctx, ctx->d_W, (int)Min, (int)Mout, (int)Mout, (int)p->kpad, (int)p->mpad, mode, p->wc,
-                                p->cs, st);
+        // W may have changed (phase / custom weights): split it again, with
+        // the correction's statistics
+        int rc = rts_group_set_w(ctx, p, ctx->d_W, (int)Mout, st);
         if (rc != RTS_OK) return rc;
     }
     p->cur = 0;
