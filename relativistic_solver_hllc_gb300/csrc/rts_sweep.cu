@@ -351,6 +351,8 @@ __device__ inline void norm_term(double old, double cur, double& loc)
     }
 }
 
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // L2 eviction priorities of the sweep's loads.  Every direction reads the
 // cells' neighbour table and medium entries (48 B per cell, 32 MB at 663,552
 // cells: they fit in L2), while the items and attenuation factors (4 B and
@@ -450,8 +452,22 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
     const uint64_t keep = l2_policy_last(), stream = l2_policy_first();
     for (int L = 0; L < ns; ++L) {
         const int i1 = steps[L + 1];
-        for (int i = steps[L] + threadIdx.x; i < i1; i += SWEEP_THREADS) {
-            const uint32_t w = ld_hint(items + i, stream);
+        // the next item's word is loaded one iteration ahead and its cell's
+        // rows prefetched into L1, so that the dependent loads of the next
+        // iteration find them (the chain word -> cell -> rows otherwise
+        // waits on memory twice per item)
+        int i = steps[L] + threadIdx.x;
+        uint32_t w_next = i < i1 ? ld_hint(items + i, stream) : 0u;
+        for (; i < i1; i += SWEEP_THREADS) {
+            const uint32_t w = w_next;
+            if (i + SWEEP_THREADS < i1) {
+                w_next = ld_hint(items + i + SWEEP_THREADS, stream);
+                const int64_t cn = w_next >> 8;
+                prefetch_l1(Il + 4 * cn);
+                prefetch_l1(a.pairs + 4 * cn);
+                prefetch_l1(a.med + 4 * cn);
+                prefetch_l1(Sd + cn);
+            }
             const int64_t c = w >> 8;
             const int f = (int)((w >> 6) & 3u);
             const double2 f01 = *reinterpret_cast<const double2*>(Il + 4 * c);
@@ -506,11 +522,16 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 7) sweep_kernel(SweepArgs a)
                     mean += node_third(a.md, unit_i, t, e3[m], sr + m, I0[m]);
                 }
             }
-            norm_term(pick(f, f01.x, f01.y, f23.x, f23.y), mean, loc);
+            const double old_f = pick(f, f01.x, f01.y, f23.x, f23.y);
+            norm_term(old_f, mean, loc);
             Il[4 * c + f] = mean;
             const int nb = pick(f, pr.x, pr.y, pr.z, pr.w);
             if (nb >= 0) {
-                norm_term(Il[nb], mean, loc);
+                // the neighbour's copy usually holds the value this face held
+                // (both were written together by the last sweep): the same
+                // term again, skipped after an integer compare of the bits
+                const double old_n = Il[nb];
+                if (__double_as_longlong(old_n) != __double_as_longlong(old_f)) norm_term(old_n, mean, loc);
                 Il[nb] = mean;
             }
         }
