@@ -76,17 +76,23 @@ def test_source_iteration_with_relaxation(ctx, prec):
 
 
 @pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
-def test_conservation_correction_of_relaxed_steps(ctx, prec):
+@pytest.mark.parametrize("M,hg", [(384, False), (1024, False), (146, True)])
+def test_conservation_correction_of_relaxed_steps(ctx, prec, M, hg):
     """tcgen05.mma rounds every FP32 accumulate toward zero, so uncorrected
     sums come out low and the loss compounds through a relaxed iteration.
     The default correction (RTS_TUNE_BIAS 0) scales each cell's integrals by
     the ratio of the conserved sum_j v_j I_j (v = W 1 in FP64) to the sum of
-    its integrals in the previous step; RTS_TUNE_BIAS -1 switches it off."""
-    N, M, lam, iters = 2048, 384, 0.9, 12
+    its integrals in the previous step; RTS_TUNE_BIAS -1 switches it off.
+    The sum of v_j S_j comes from one extra output column: at M = 1024 it
+    takes a tile of its own, at M = 146 it shares the last 8-column block
+    with real out-directions (and Henyey-Greenstein g = 0.8 spreads v most)."""
+    N, lam, iters = 2048, 0.9, 12
     xyz, area, fa, il, B = problem(N, M, seed=4, sigma=1.5)
-    W = oracle.weights_thomson(xyz, area, fa)
+    W = oracle.weights_hg(xyz, area, 0.8) if hg else oracle.weights_thomson(xyz, area, fa)
     S_ref, _, _ = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
     ctx.init(xyz, area, fa, N)
+    if hg:
+        ctx.set_phase(PHASE_HG, 0.8)
     stats = {}
     try:
         for mode in (-1, 0):
@@ -106,6 +112,36 @@ def test_conservation_correction_of_relaxed_steps(ctx, prec):
     assert on[1] <= TOL[prec]
     with pytest.raises(Exception):
         ctx.set_tuning(TUNE_BIAS, -2)
+
+
+def test_correction_follows_a_change_of_w(ctx):
+    """An iteration set up again after a change of phase kernel (same sizes:
+    the problem is reused) recomputes the correction's statistics of W with
+    the split W rows."""
+    N, M, lam, iters = 2048, 302, 0.9, 12
+    xyz, area, fa, il, B = problem(N, M, seed=6, sigma=1.5)
+    ctx.init(xyz, area, fa, N)
+    ctx.copy_illum(il)
+    ctx.solve_setup("fp16x3", B, lam)
+    ctx.solve_step(True)
+    ctx.set_phase(PHASE_HG, 0.6)
+
+    def run():
+        ctx.copy_illum(il)
+        ctx.solve_setup("fp16x3", B, lam)
+        for _ in range(iters):
+            ctx.solve_step_async(True)
+        ctx.wait()
+        return ctx.solve_read()
+
+    S_reused = run()
+    ctx.init(xyz, area, fa, N)  # a fresh problem, set up with the new kernel from the start
+    ctx.set_phase(PHASE_HG, 0.6)
+    S_fresh = run()
+    assert np.array_equal(S_reused, S_fresh)
+    W = oracle.weights_hg(xyz, area, 0.6)
+    S_ref, _, _ = oracle.iterate(W, oracle.face_mean(il, N, M), B, lam, iters, True)
+    assert float(np.max(np.abs(S_reused - S_ref) / S_ref)) <= TOL["fp16x3"]
 
 
 @pytest.mark.parametrize("prec", ["fp16x3", "bf16x3", "tf32x3"])

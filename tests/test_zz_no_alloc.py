@@ -71,3 +71,34 @@ def test_noalloc_rejects_oversized_direction_sets(native_lib):
     # before anything is launched, as is a misaligned output
     assert fn(p + 8, p, p, 1, 4, 1.0, p, None) == _native.ERR_INVALID_ARGUMENT
     assert fn(p, p, p, 1, 4, 1.0, p + 4, None) == _native.ERR_INVALID_ARGUMENT
+
+
+def test_noalloc_in_a_captured_graph(native_lib):
+    """The entry point allocates nothing and synchronises nothing, so it can be
+    captured into a CUDA graph on the caller's stream (after a first call on
+    the device outside the capture); the replay gives the eager result."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    fn = native_lib.rts_scattering_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
+    N, M = 2500, 64
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(23, 0.0, 1.2, N, M, independent_faces=True)
+    d_il, d_xyz, d_area = _dev(torch, il), _dev(torch, xyz), _dev(torch, area)
+    eager = torch.zeros(M * N, dtype=torch.float64, device="cuda")
+    graphed = torch.full((M * N,), float("nan"), dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+    args = (d_il.data_ptr(), d_xyz.data_ptr(), d_area.data_ptr(), N, M, fa)
+    with torch.cuda.stream(side):
+        assert fn(*args, eager.data_ptr(), side.cuda_stream) == _native.OK  # first call outside a capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        rc = fn(*args, graphed.data_ptr(), side.cuda_stream)
+    assert rc == _native.OK
+    g.replay()
+    torch.cuda.synchronize()
+    a, b = eager.cpu().numpy(), graphed.cpu().numpy()
+    assert float(np.max(np.abs(a - b) / np.abs(a))) <= TOL
