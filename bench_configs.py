@@ -320,7 +320,8 @@ def config5(pkg, native, ctx, torch, loads=(0.1, 0.5, 0.8, 1.0, 1.2), window_s=2
     mean_work = np.mean([N * M * it for (_, N, M, _, it) in pop])
     results = {"saturation_cell_dir_iter_per_s": sat, "saturation_requests": len(sat_specs),
                "policy": {0: "all resident", 1: "earliest deadline first within a tile budget",
-                          2: "least remaining work first within a tile budget"}[policy],
+                          2: "least remaining work first within a tile budget",
+                          3: "first come first served within a tile budget"}[policy],
                "tile_budget": budget or "8 waves",
                "loads": []}
     for f in loads:

@@ -603,11 +603,14 @@ int rts_illum_solve(rts_ctx* ctx, int precision, int max_iter, double accuracy, 
 #define RTS_TUNE_BIAS 2
 /*   RTS_TUNE_SERVE_POLICY: how rts_serve_run chooses the requests a step
  *   advances: 1 (default) earliest deadline first, the deadline being arrival
- *   + 2 x the request's estimated solve time alone; 2 least remaining work
- *   first, a request left out gaining priority with every step it waits;
- *   both within a tile budget; 0 every resident request every step.
+ *   + RTS_TUNE_SERVE_SLACK/100 x the request's estimated solve time alone; 2
+ *   least remaining work first, a request left out gaining priority with
+ *   every step it waits; 3 first come first served (the oldest request's
+ *   whole step first, later ones only in the budget it leaves: a request
+ *   whose step fills the budget runs alone); 1 to 3 within a tile budget; 0
+ *   every resident request every step.
  *   RTS_TUNE_SERVE_BUDGET: tiles (128 cells x up to 256 directions) per step
- *   under policies 1 and 2; 0 = 8 waves of the SMs.  At least one request
+ *   under policies 1 to 3; 0 = 8 waves of the SMs.  At least one request
  *   always runs. */
 /*   RTS_TUNE_SERVE_SLACK: policy 1's deadline, arrival + slack/100 x the
  *   request's estimated solve time alone (0 = 500). */

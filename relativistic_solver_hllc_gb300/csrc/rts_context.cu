@@ -859,7 +859,7 @@ int rts_set_tuning(rts_ctx* ctx, int key, int value)
         ctx->split_flush = value;
         return RTS_OK;
     case RTS_TUNE_SERVE_POLICY:
-        RTS_REQUIRE(ctx, value >= 0 && value <= 2, RTS_ERR_INVALID_ARGUMENT, "serving policy %d not 0, 1 or 2", value);
+        RTS_REQUIRE(ctx, value >= 0 && value <= 3, RTS_ERR_INVALID_ARGUMENT, "serving policy %d not 0 to 3", value);
         ctx->serve_policy = value;
         return RTS_OK;
     case RTS_TUNE_SERVE_SLACK:

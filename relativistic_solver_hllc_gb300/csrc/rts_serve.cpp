@@ -308,6 +308,7 @@ extern "C" int rts_serve_run(rts_ctx* ctx, const rts_request* reqs, int64_t n, i
         if (ctx->serve_policy != 0) {
             auto key = [&](size_t i) {
                 if (ctx->serve_policy == 1) return active[i].deadline;
+                if (ctx->serve_policy == 3) return reqs[active[i].req].arrival_s;
                 return active[i].step_work * active[i].remaining / (1.0 + active[i].waited);
             };
             std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return key(x) < key(y); });
