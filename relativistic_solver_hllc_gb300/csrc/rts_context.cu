@@ -407,6 +407,9 @@ int rts_send_illum_async(rts_ctx* ctx, int64_t size, int64_t shift_dev, int64_t 
                                       rts_bytes<double>(size), cudaMemcpyHostToDevice,
                                       ctx->streams[RTS_STREAM_SCATTERING_1]));
     rts_inputs_changed(ctx);
+    // at a tensor precision the integral calls' face sums start as the
+    // directions arrive
+    if (ctx->call_precision != RTS_PREC_FP64) return rts_split_eager_send(ctx, shift_dev, size);
     return RTS_OK;
 }
 

@@ -91,6 +91,14 @@ struct rts_split_state {
     cudaEvent_t ev_prep = nullptr;            // on the preparing slot's stream: rows ready
     cudaEvent_t ev_use[RTS_STREAM_COUNT] = {};  // on each slot's stream: its contraction queued
     bool use_recorded[RTS_STREAM_COUNT] = {};
+    // ... and their face sums computed while the Illum arrives: whole
+    // directions copied by rts_send_illum_async in order from direction 0,
+    // each summed on eager_st right after its copy
+    cudaStream_t eager_st = nullptr;
+    cudaEvent_t ev_sent = nullptr, ev_eager = nullptr;
+    int64_t eager_next = -1;     // directions [0, eager_next) summed so far; -1: none
+    int64_t eager_version = -1;  // inputs_version right after the last of those copies
+    int eager_mode = -1;
 };
 
 // Device state of the transport sweep (rts_sweep.cu): the mesh, the
@@ -276,6 +284,14 @@ int rts_pp_rows_from_f32(rts_ctx* ctx, const float* ibar, int64_t N, int M, int6
 int rts_pp_rows_from_faces_staged(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad,
                                   const double* B, int mode, float* rs, int64_t npad, uint16_t* A, double* sums,
                                   unsigned long long* cmax, cudaStream_t st, bool bound = false);
+// Its two halves: the face sums of directions [j0, j1) (merging their maxima
+// into cmax when non-null; cmax zeroed by the caller), and the scales and the
+// split from the sums of all M directions.
+int rts_pp_face_sums(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int j0, int j1, double* sums,
+                     unsigned long long* cmax, cudaStream_t st);
+int rts_pp_rows_from_sums(rts_ctx* ctx, int64_t N, int M, int kpad, const double* B, int mode, float* rs, int64_t npad,
+                          uint16_t* A, const double* sums, const unsigned long long* cmax, cudaStream_t st,
+                          bool bound = false);
 int rts_pp_join_rows(rts_ctx* ctx, const uint16_t* A, int64_t N, int M, int64_t rows, int kpad, const float* rs_inv,
                      int mode, double* out, cudaStream_t st);
 int rts_pp_f32_to_f64(rts_ctx* ctx, const float* s, double* d, int64_t n, cudaStream_t st);
@@ -323,6 +339,10 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st);
 // [start, end) of the FP64 device S on `st`, with the split operands of
 // stream slot `slot` (no host copies, no host synchronisation once set up).
 int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int slot, cudaStream_t st);
+// After a copy of [shift_dev, shift_dev + size) of the device Illum queued on
+// the scattering stream at a tensor precision: the face sums of the directions
+// it completes, on a stream of their own (rts_split.cu).
+int rts_split_eager_send(rts_ctx* ctx, int64_t shift_dev, int64_t size);
 int rts_split_read(rts_ctx* ctx, double* S_host);
 int rts_split_read_ibar(rts_ctx* ctx, double* ibar_host);
 void rts_split_free(rts_ctx* ctx);

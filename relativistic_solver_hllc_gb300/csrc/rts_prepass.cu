@@ -211,13 +211,13 @@ __device__ __forceinline__ float pow2_scaled_to_f32(double x, int k)
 // FP64 work is the 3 adds of the sum.  Thread per (cell, 32 directions): a
 // warp reads 1 KB and writes 256 B contiguous per direction, no transpose.
 __global__ void __launch_bounds__(256) face_sums_kernel(const double* __restrict__ illum, int64_t N, int64_t ld,
-                                                        int M, double* __restrict__ sums,
+                                                        int jb, int je, double* __restrict__ sums,
                                                         unsigned long long* __restrict__ cmax)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= N) return;
-    const int j0 = blockIdx.y * 32;
-    const int j1 = min(M, j0 + 32);
+    const int j0 = jb + blockIdx.y * 32;  // directions [jb, je) of the launch, 32 per block row
+    const int j1 = min(je, j0 + 32);
     unsigned long long mx = 0;
 #pragma unroll 8
     for (int j = j0; j < j1; ++j) {
@@ -466,17 +466,33 @@ int rts_pp_rows_from_faces(rts_ctx* ctx, const double* illum, int64_t N, int64_t
     return RTS_OK;
 }
 
+int rts_pp_face_sums(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int j0, int j1, double* sums,
+                     unsigned long long* cmax, cudaStream_t st)
+{
+    if (j1 <= j0) return RTS_OK;
+    face_sums_kernel<<<dim3((unsigned)((N + 255) / 256), (unsigned)((j1 - j0 + 31) / 32)), 256, 0, st>>>(
+        illum, N, ld, j0, j1, sums, cmax);
+    RTS_CHECK_LAUNCH(ctx, "face_sums_kernel");
+    ctx->launches++;
+    return RTS_OK;
+}
+
 int rts_pp_rows_from_faces_staged(rts_ctx* ctx, const double* illum, int64_t N, int64_t ld, int M, int kpad,
                                   const double* B, int mode, float* rs, int64_t npad, uint16_t* A, double* sums,
                                   unsigned long long* cmax, cudaStream_t st, bool bound)
 {
+    const bool scaled = mode == 1 || bound;
+    if (scaled) RTS_CUDA_TRY(ctx, cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned long long), st));
+    int rc = rts_pp_face_sums(ctx, illum, N, ld, 0, M, sums, scaled ? cmax : nullptr, st);
+    if (rc != RTS_OK) return rc;
+    return rts_pp_rows_from_sums(ctx, N, M, kpad, B, mode, rs, npad, A, sums, cmax, st, bound);
+}
+
+int rts_pp_rows_from_sums(rts_ctx* ctx, int64_t N, int M, int kpad, const double* B, int mode, float* rs, int64_t npad,
+                          uint16_t* A, const double* sums, const unsigned long long* cmax, cudaStream_t st, bool bound)
+{
     const bool fp16 = mode == 1;
     const bool scaled = fp16 || bound;
-    if (scaled) RTS_CUDA_TRY(ctx, cudaMemsetAsync(cmax, 0, (size_t)N * sizeof(unsigned long long), st));
-    face_sums_kernel<<<dim3((unsigned)((N + 255) / 256), (unsigned)((M + 31) / 32)), 256, 0, st>>>(
-        illum, N, ld, M, sums, scaled ? cmax : nullptr);
-    RTS_CHECK_LAUNCH(ctx, "face_sums_kernel");
-    ctx->launches++;
     if (scaled) {
         rowscale_from_max_kernel<<<(unsigned)((npad + 127) / 128), 128, 0, st>>>(cmax, N, B, rs, npad);
         RTS_CHECK_LAUNCH(ctx, "rowscale_from_max_kernel");

@@ -301,6 +301,7 @@ static void free_call_rows(rts_ctx* ctx)
     s.call_gen++;
     s.call_version = -1;
     s.prep_slot = -1;
+    s.eager_next = -1;
 }
 
 // The shared rows for (N, M, mode): allocated on first use and when the
@@ -342,6 +343,53 @@ static int record_on(rts_ctx* ctx, cudaEvent_t& ev, cudaStream_t st)
 {
     if (!ev) RTS_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     RTS_CUDA_TRY(ctx, cudaEventRecord(ev, st));
+    return RTS_OK;
+}
+
+int rts_split_eager_send(rts_ctx* ctx, int64_t shift_dev, int64_t size)
+{
+    rts_split_state& s = ctx->split;
+    if (ctx->cc_major != 10) return RTS_OK;
+    const int64_t per = 4 * ctx->N, M = ctx->M;
+    const int mode = rts_split_mode(ctx->call_precision);
+    const int64_t j0 = shift_dev / per, j1 = (shift_dev + size) / per;
+    const bool whole = size > 0 && shift_dev % per == 0 && size % per == 0 && j1 <= M;
+    // a sequence runs from direction 0, each direction once and in order,
+    // with nothing else written in between (the copy itself bumped the version)
+    const bool next = whole && j0 > 0 && j0 == s.eager_next && s.eager_mode == mode &&
+                      s.eager_version == ctx->inputs_version - 1;
+    if (!whole || (j0 != 0 && !next)) {
+        s.eager_next = -1;  // this Illum is prepared whole at the call
+        return RTS_OK;
+    }
+    int bn, n_tiles;
+    int64_t kpad, mpad, rows_pad, m_tiles;
+    rts_group_geometry(M, M, ctx->N, 0, &bn, &n_tiles, &kpad, &mpad, &rows_pad, &m_tiles);
+    int rc = ensure_call_rows(ctx, mode, rows_pad, (mode == 2 ? 4 : 2) * kpad);
+    if (rc != RTS_OK) return rc;
+    if (!s.eager_st) RTS_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s.eager_st, cudaStreamNonBlocking));
+    cudaStream_t s1 = ctx->streams[RTS_STREAM_SCATTERING_1];
+    if (j0 == 0) {
+        // a new sequence: the staging may still be read by a preparation or
+        // contraction queued before
+        if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(s.eager_st, s.ev_prep, 0));
+        for (int i = 0; i < RTS_STREAM_COUNT; ++i)
+            if (s.use_recorded[i]) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(s.eager_st, s.ev_use[i], 0));
+        if (mode == 1)
+            RTS_CUDA_TRY(ctx, cudaMemsetAsync(s.call_max, 0, (size_t)ctx->N * sizeof(unsigned long long), s.eager_st));
+    }
+    if ((rc = record_on(ctx, s.ev_sent, s1)) != RTS_OK) return rc;
+    RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(s.eager_st, s.ev_sent, 0));
+    rc = rts_pp_face_sums(ctx, ctx->d_illum, ctx->N, ctx->N, (int)j0, (int)j1, s.call_sums,
+                          mode == 1 ? s.call_max : nullptr, s.eager_st);
+    if (rc == RTS_OK) rc = record_on(ctx, s.ev_eager, s.eager_st);
+    if (rc != RTS_OK) {
+        s.eager_next = -1;
+        return rc;
+    }
+    s.eager_next = j1;
+    s.eager_mode = mode;
+    s.eager_version = ctx->inputs_version;
     return RTS_OK;
 }
 
@@ -399,12 +447,19 @@ int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int
         s.prep_served[slot] = true;
     } else {
         // the rows and the staging may still be read by contractions queued
-        // on the other slots
+        // on the other slots, and the staging written by face sums in flight
         for (int i = 0; i < RTS_STREAM_COUNT; ++i)
             if (i != slot && s.use_recorded[i]) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_use[i], 0));
+        if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
         s.call_version = -1;
-        rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum, N, N, (int)M, (int)kpad, nullptr, mode, s.call_rs,
-                                           rows_pad, s.call_a, s.call_sums, s.call_max, st);
+        // the face sums of this Illum, when its copies summed every direction
+        const bool eager = s.eager_next == M && s.eager_mode == mode && s.eager_version == ctx->inputs_version;
+        if (eager)
+            rc = rts_pp_rows_from_sums(ctx, N, (int)M, (int)kpad, nullptr, mode, s.call_rs, rows_pad, s.call_a,
+                                       s.call_sums, s.call_max, st);
+        else
+            rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum, N, N, (int)M, (int)kpad, nullptr, mode, s.call_rs,
+                                               rows_pad, s.call_a, s.call_sums, s.call_max, st);
         if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
         if (rc != RTS_OK) return rc;
         s.call_version = ctx->inputs_version;
@@ -458,6 +513,12 @@ void rts_split_free(rts_ctx* ctx)
     if (s.ev_prep) cudaEventDestroy(s.ev_prep);
     for (cudaEvent_t e : s.ev_use)
         if (e) cudaEventDestroy(e);
+    if (s.ev_sent) cudaEventDestroy(s.ev_sent);
+    if (s.ev_eager) cudaEventDestroy(s.ev_eager);
+    if (s.eager_st) {
+        cudaStreamSynchronize(s.eager_st);
+        cudaStreamDestroy(s.eager_st);
+    }
     for (int i = 0; i < RTS_HOST_CHUNKS; ++i) {
         rts_group_batch_free(s.chunk[i]);
         if (s.ev_in[i]) cudaEventDestroy(s.ev_in[i]);

@@ -70,3 +70,51 @@ def test_staged_rows_match_direct_rows(ctx, prec, M):
     normal[np.random.default_rng(17).permutation(N)[:128]] = False
     rel = np.abs(S_sync[:, normal] - ref[:, normal]) / np.abs(ref[:, normal])
     assert float(rel.max()) <= (1e-4 if prec == "bf16x3" else 1e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
+def test_face_sums_while_the_illum_arrives(ctx, prec):
+    """Whole directions copied in order from direction 0 (the reference's
+    per-direction CudaSendIllumAsync) are summed as they arrive; the pair of
+    calls then only scales and splits.  The result is the whole preparation's
+    bit for bit, and copies in another order, in pieces that are not whole
+    directions, or followed by another write fall back to it."""
+    N, M = 4099, 75
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(31, 0.0, 1.5, N, M, independent_faces=True)
+    ctx.init(xyz, area, fa, N)
+    ctx.set_precision(prec)
+
+    def pair():
+        out1, out2 = np.zeros(M * N), np.zeros(M * N)
+        ctx.scattering_async(0, M // 3, STREAM_SCATTERING_1, out1)
+        ctx.scattering_async(0, M, STREAM_SCATTERING_2, out2)
+        ctx.wait()
+        assert np.array_equal(out1[: (M // 3) * N], out2[: (M // 3) * N])
+        return out2
+
+    try:
+        ctx.copy_illum(il)
+        whole = pair()
+        runs = {}
+        for j in range(M):  # in order, one direction per copy
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il)
+        runs["in order"] = pair()
+        for j0 in range(0, M, 4):  # in order, several directions per copy
+            n = min(4, M - j0)
+            ctx.send_illum_async(4 * N * n, 4 * N * j0, 4 * N * j0, il)
+        runs["in order, 4 per copy"] = pair()
+        for j in reversed(range(M)):
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il)
+        runs["reversed"] = pair()
+        for j in range(2 * M):  # half directions
+            ctx.send_illum_async(2 * N, 2 * N * j, 2 * N * j, il)
+        runs["halves"] = pair()
+        for j in range(M):
+            ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il)
+        ctx.copy_illum(il)  # another write after the copies
+        runs["then a copy"] = pair()
+    finally:
+        ctx.set_precision("fp64")
+    for name, S in runs.items():
+        assert np.array_equal(S, whole), name
