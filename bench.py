@@ -621,14 +621,18 @@ def run_ours(args, rank, world, local):
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    per_step = []
     for _ in range(Ke):
+        ts = time.perf_counter()
         reference_sequence()
+        per_step.append(time.perf_counter() - ts)
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, dist)
     ctx.set_precision("fp64")
     e2e = {"value": N * M * Ke * world / e2e_s / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": M * N * 4 * 8, "d2h_bytes_per_step": (size_1 + M) * N * 8,
            "steps": Ke, "ms_per_step": e2e_s / Ke * 1e3,
+           "ms_per_step_median": statistics.median(per_step) * 1e3, "ms_per_step_min": min(per_step) * 1e3,
            "call": f"the reference's calling sequence at {prec}: {M} x rts_send_illum_async (CudaSendIllumAsync, "
                    f"pinned host Illum), rts_scattering_async [0,{size_1}) on stream 1 and [0,{M}) on stream 2 "
                    "(CalculateIntScatteringAsyncMPIStream x 2, D2H of S into the pinned host array), "
@@ -643,12 +647,17 @@ def run_ours(args, rank, world, local):
     ctx.scattering_update(prec, illum_host, B_host, lam, S_host)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    per_call = []
     for _ in range(Ke):
+        ts = time.perf_counter()
         ctx.scattering_update(prec, illum_host, B_host, lam, S_host)
+        per_call.append(time.perf_counter() - ts)
     e2e2_s = max_over_ranks(time.perf_counter() - t0, dist)
     h2d, d2h = M * N * 4 * 8 + N * 8, M * N * 8
     e2e_host_call = {"value": N * M * Ke * world / e2e2_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                      "d2h_bytes_per_step": d2h, "steps": Ke, "ms_per_step": e2e2_s / Ke * 1e3,
+                     "ms_per_step_median": statistics.median(per_call) * 1e3,
+                     "ms_per_step_min": min(per_call) * 1e3,
                      "link_gbs": (h2d + d2h) / (e2e2_s / Ke) / 1e9,
                      "call": "rts_scattering_update (pinned host buffers, 16 cell ranges pipelined)"}
 
