@@ -118,3 +118,29 @@ def test_face_sums_while_the_illum_arrives(ctx, prec):
         ctx.set_precision("fp64")
     for name, S in runs.items():
         assert np.array_equal(S, whole), name
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "tf32x3"])
+def test_shard_of_out_directions_at_tensor_precision(ctx, prec):
+    """InitDevice(start, end) shards the out-directions (d_GetS_MPI): the pair
+    of calls over the local range at a tensor precision, after whole-direction
+    copies in order, against the oracle's integral of the same shard."""
+    N, M = 2000, 90
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(33, 0.0, 1.2, N, M, independent_faces=True)
+    for start, end in [(0, 90), (17, 61), (89, 90)]:
+        loc = end - start
+        ctx.init(xyz, area, fa, N, start, end)
+        ctx.set_precision(prec)
+        try:
+            for j in range(M):
+                ctx.send_illum_async(4 * N, 4 * N * j, 4 * N * j, il)
+            out1, out2 = np.zeros(loc * N), np.zeros(loc * N)
+            ctx.scattering_async(0, loc // 3, STREAM_SCATTERING_1, out1)
+            ctx.scattering_async(0, loc, STREAM_SCATTERING_2, out2)
+            ctx.wait()
+        finally:
+            ctx.set_precision("fp64")
+        ref = oracle.calculate_int_cpu(N, xyz, area, fa, il, start, loc)
+        assert float(np.max(np.abs(out2.reshape(loc, N) - ref) / np.abs(ref))) <= 1e-5, (start, end)
+        assert np.array_equal(out1[: (loc // 3) * N], out2[: (loc // 3) * N])
