@@ -300,8 +300,9 @@ int rts_group_reset_energy(rts_ctx* ctx, GProb* p, cudaStream_t st)
 {
     if (!p->delta) return RTS_OK;
     RTS_CUDA_TRY(ctx, cudaMemsetAsync(p->delta, 0, (size_t)(p->rows_pad * 4), st));
-    group_energy_init_kernel<<<(unsigned)((p->rows + 127) / 128), 128, 0, st>>>(p->a[p->cur], p->rows, (int)p->kpad,
-                                                                             (int)p->M, p->mode, p->vrow, p->rs, p->ex);
+    group_energy_init_kernel<<<(unsigned)((p->rows * 32 + 255) / 256), 256, 0, st>>>(p->a[p->cur], p->rows, (int)p->kpad,
+                                                                                  (int)p->M, p->mode, p->vrow, p->rs,
+                                                                                  p->ex);
     RTS_CHECK_LAUNCH(ctx, "group_energy_init_kernel");
     ctx->launches++;
     return RTS_OK;

@@ -719,29 +719,33 @@ __global__ void group_energy_kernel(const GroupProblem* __restrict__ probs, int 
 
 // sum_j v_j x_j of every row of the current split input, in the quanta of
 // energy_scale (FP64, once per set-up of an iteration): the split values
-// joined as the tensor core multiplies them (hi + lo).
+// joined as the tensor core multiplies them (hi + lo).  A warp per row, its
+// lanes on consecutive columns (coalesced), FP64 lane sums reduced in a fixed
+// shuffle order.
 __global__ void group_energy_init_kernel(const uint16_t* __restrict__ A, int64_t rows, int kpad, int M, int mode,
                                          const float* __restrict__ vrow, const float* __restrict__ rs, double* ex)
 {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= rows) return;  // r is uniform over the warp
     float q = vrow[kpad] * (mode == 1 ? 1.0f : rs[r]);
     if (!(q > 0.0f && q < 3.0e38f)) q = 0.0f;
     double s = 0.0;
     if (mode == 2) {
         const float* row = reinterpret_cast<const float*>(A + r * 4 * (int64_t)kpad);
-        for (int j = 0; j < M; ++j) {
+        for (int j = lane; j < M; j += 32) {
             const int h = (j >> 4) * 32 + (j & 15);
             s += (double)vrow[j] * (double)(row[h] + row[h + 16]);
         }
     } else {
         const uint16_t* row = A + r * 2 * (int64_t)kpad;
-        for (int j = 0; j < M; ++j) {
+        for (int j = lane; j < M; j += 32) {
             const int64_t h = rts_ptx::ilv_hi(j);
             s += (double)vrow[j] * (double)rts_ptx::join_any(mode == 1, row[h], row[h + 32]);
         }
     }
-    ex[r] = s * (double)q;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) ex[r] = s * (double)q;
 }
 
 // Flip the ping-pong Ibar buffer of every problem whose relaxed step ended in
