@@ -6,13 +6,13 @@
 // of different cell and direction counts, phase kernels and precisions) form
 // one list that persistent CTAs (one per SM) walk with a fixed stride.
 //
-// Measured on GB300: a warp that issues tcgen05.mma back to back gets one
-// instruction through every ~300 cycles, whatever N (32..256) or the
-// accumulator is, while the SM's tensor core sustains about four such
-// streams of N = 128 (or two of N = 256).  So a CTA runs two issuing warps,
-// each with N up to 256, on alternate chunks of the in-direction range of the
-// same tile (split K inside the CTA): together they keep the tensor core
-// near its peak while each accumulator is drained in turn.
+// Measured on GB300: one thread issuing M = 128, N = 256 MMAs back to back
+// reaches 0.83 of the SM's tensor rate, two threads with an accumulator each
+// its full rate.  A CTA runs two issuing warps, each with N up to 256, on
+// alternate chunks of the in-direction range of the same tile (split K
+// inside the CTA), so that each accumulator is drained while the other
+// fills; of the issue schemes measured (one issuer for both accumulators,
+// both issuers on every chunk with a column half each) this was the fastest.
 //
 // Warp roles (19 warps, 608 threads, one CTA per SM):
 //   warp 0       TMA producer: A (split Ibar rows) and B (split W rows)
