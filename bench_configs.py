@@ -103,7 +103,8 @@ def timed_steps(ctx, fn, steps, torch, stream_handle):
 # ---------------------------------------------------------------- configurations
 def config3(pkg, native, ctx, torch, steps, warmup, precision):
     N, M, G, g = 300_000, 590, 8, 0.7
-    tuned = ctx.autotune(M, precision)  # tile width for M = 590 (not timed)
+    # schedule for M = 590 at this cell count (not timed)
+    best, tried = ctx.autotune_schedule(M, precision, cells=N * G)
     lam = np.array([0.3 + 0.08 * i for i in range(G)])
     desc = native.problem_desc(N, M, G, 1, g, precision)
     b = native.Batch(ctx)
@@ -124,7 +125,7 @@ def config3(pkg, native, ctx, torch, steps, warmup, precision):
             "max_rel_err": mx, "mean_rel_err": mean, "precision": precision,
             "workload": "300,000 cells x 590 directions x 8 groups, HG g=0.7 row-normalised, lognormal(0,1) FP32, "
                         "lambda_g=0.3+0.08g",
-            "autotuned_bn": tuned[0], "autotune_ms": {str(k): v for k, v in tuned[2].items()}}
+            "autotuned": {x: best[x] for x in ("flush", "bn", "order", "ms")}, "schedules_timed": len(tried)}
 
 
 def moments_pass(pkg, native, ctx, torch, steps, warmup, N=663_552):
