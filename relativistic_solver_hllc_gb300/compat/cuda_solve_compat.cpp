@@ -30,7 +30,13 @@
 // asynchronous calls on the device-resident Illum that the source iteration
 // makes (CalculateIntScatteringAsyncMPIStream, ...AsyncMPI, ...Async) and the
 // synchronous CalculateIntScattering -- runs the split tcgen05 path, to
-// <= 1e-6 relative for fp16x3 and tf32x3.
+// <= 1e-6 relative for fp16x3 and tf32x3.  At a tensor precision the
+// RTS_SCATTER_TUNE environment variable may name a schedule table file: when
+// the file exists InitDevice loads it (rts_autotune_load); when it does not,
+// InitDevice runs the schedule autotuner once for this rank's directions and
+// cells (rts_autotune_schedule) and writes the table there, so later runs of
+// the solver start from it.  The schedule changes the speed of the calls;
+// within the accuracy above, not their results.
 //
 // Cell geometry: like the reference's InitDevice (cuda/cuda_struct.cu:134-176),
 // the first rank reads normals.bin, squares.bin and volume.bin from the
@@ -75,6 +81,23 @@ int report(int rc, const char* where)
     if (rc != RTS_OK)
         std::fprintf(stderr, "%s failed: status %d: %s\n", where, rc, g_ctx ? rts_last_error(g_ctx) : "");
     return rc == RTS_OK ? 0 : 1;
+}
+
+// RTS_SCATTER_TUNE: load the schedule table, or tune and write it
+void tune_schedule(int precision, int M, int64_t cells)
+{
+    const char* path = std::getenv("RTS_SCATTER_TUNE");
+    if (!path || !*path || precision == RTS_PREC_FP64) return;
+    if (std::FILE* f = std::fopen(path, "r")) {
+        std::fclose(f);
+        report(rts_autotune_load(g_ctx, path), "InitDevice (schedule table)");
+        return;
+    }
+    rts_tune_choice best;
+    if (report(rts_autotune_schedule(g_ctx, M, precision, cells, &best, nullptr, 0, nullptr),
+               "InitDevice (schedule autotuner)"))
+        return;
+    report(rts_autotune_save(g_ctx, path), "InitDevice (schedule table)");
 }
 
 rts_stream_id stream_of(e_cuda_stream_id_t s)
@@ -154,7 +177,9 @@ void InitDevice(const grid_directions_t& grid_dir_host, grid_t& grid_host, const
         return;
     rts_host_illum(g_ctx, &grid_host.Illum);
     rts_host_scattering(g_ctx, &grid_host.scattering);
-    report(rts_set_precision(g_ctx, env_precision()), "InitDevice (precision)");
+    const int precision = env_precision();
+    if (report(rts_set_precision(g_ctx, precision), "InitDevice (precision)") == 0)
+        tune_schedule(precision, M, grid_host.size);
     if (start == 0) {  // the first rank also receives the moments (cuda/cuda_struct.cu:158-175)
         grid_host.divstream = new Type[grid_host.size]();
         grid_host.divimpuls = new Vector3[grid_host.size]();

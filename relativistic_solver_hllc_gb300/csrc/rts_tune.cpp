@@ -320,7 +320,7 @@ extern "C" int rts_autotune_save(rts_ctx* ctx, const char* path)
     RTS_REQUIRE(ctx, f, RTS_ERR_INVALID_ARGUMENT, "cannot write %s", path);
     std::fprintf(f, "# rts schedule table: M precision flush cell_bucket bn order ms\n");
     for (const rts_tune_entry& e : ctx->tune)
-        std::fprintf(f, "%lld %d %d %d %d %d %.6f\n", (long long)e.M, e.precision, e.flush, e.bucket, e.bn, e.order,
+        std::fprintf(f, "%lld %d %d %d %d %d %.9g\n", (long long)e.M, e.precision, e.flush, e.bucket, e.bn, e.order,
                      e.ms);
     const bool ok = std::fclose(f) == 0;
     RTS_REQUIRE(ctx, ok, RTS_ERR_INVALID_ARGUMENT, "error writing %s", path);

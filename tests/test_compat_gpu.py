@@ -129,3 +129,33 @@ def test_calling_sequence_at_tensor_precision(native_lib, tmp_path, prec):
     # output), and equal the synchronous call's, which splits the cells into
     # ranges instead
     assert np.array_equal(S_async, S_sync)
+
+
+@pytest.mark.gpu
+def test_schedule_table_through_the_shim(native_lib, tmp_path):
+    """RTS_SCATTER_TUNE at a tensor precision: the first run of the solver
+    tunes the schedule at InitDevice and writes the table; the second loads
+    it.  Both runs choose the same schedule, so they give the same values,
+    within 1e-6 of the oracle."""
+    exe = build_driver(tmp_path)
+    N, M = 3000, 200
+    xyz, area, fa = oracle.fibonacci_directions(M)
+    il = oracle.illum(24, 0.0, 1.5, N, M, independent_faces=True)
+    table = tmp_path / "schedule.txt"
+    env = {"RTS_SCATTER_PRECISION": "fp16x3", "RTS_SCATTER_TUNE": str(table)}
+    runs = []
+    for k in range(2):
+        d = tmp_path / f"run{k}"
+        d.mkdir()
+        runs.append(_run_driver(exe, d, xyz, area, fa, il, N, 25, env))
+        assert table.exists()
+        if k == 0:
+            first = table.read_text()
+    assert table.read_text() == first  # the second run loaded it, wrote nothing
+    rows = [ln.split() for ln in first.splitlines() if ln and not ln.startswith("#")]
+    assert rows and all(len(r) == 7 and int(r[0]) == M and int(r[1]) == _native.PREC_FP16X3 for r in rows)
+    ref = oracle.calculate_int_cpu(N, xyz, area, fa, il)
+    for S in runs[0]:
+        assert float(np.max(np.abs(S - ref) / ref)) <= 1e-6
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
