@@ -12,7 +12,8 @@
 // The reference kernel gives each thread one (cell, out-direction) pair and
 // loops over all in-directions, re-reading the 4 faces and recomputing Gamma
 // for every pair and accumulating straight into global memory.  Here a CTA
-// owns a 128-cell x 64-out-direction tile: the face mean is taken once per
+// owns a 128-cell x 64-out-direction tile (the out-directions left over
+// past a multiple of 64 take one narrower tile): the face mean is taken once per
 // (in-direction, cell) while the tile of Ibar is staged in shared memory, W
 // (FP64, precomputed once) is staged beside it, and each thread keeps an
 // 8-cell x 4-direction block of accumulators in registers.  GB300 FP64 runs
@@ -45,23 +46,27 @@ __device__ __forceinline__ void residual_max(unsigned long long* dst, double v)
         atomicMax(dst, (unsigned long long)__double_as_longlong(v));
 }
 
-template <bool kUpdate, bool kResidual>
-__global__ void __launch_bounds__(F64_THREADS)
-scatter_fp64_kernel(const double* __restrict__ illum, const double* __restrict__ W, int64_t N,
-                    int M, int ldw, int k_begin, int k_end, double* __restrict__ S,
-                    const double* __restrict__ B, double lambda,
-                    unsigned long long* __restrict__ resid)
+// One tile of 128 cells x 16*NB out-directions [k0, k0 + 16*NB): each
+// thread keeps 8 cells x NB directions of accumulators.  Every output is the
+// same FMA chain over the in-directions in order whatever NB, so a tile's
+// width changes no result.  GB300's FP64 pipe retires about two FMAs per SM
+// per cycle, far below the shared-memory loads that feed them, so a narrow
+// tile costs about NB/4 of a full one.
+template <bool kUpdate, bool kResidual, int NB>
+__device__ __forceinline__ void scatter_tile(double (*sI)[F64_TC], double (*sW)[F64_TK],
+                                             const double* __restrict__ illum, const double* __restrict__ W,
+                                             int64_t N, int M, int ldw, int k0, int k_end, double* __restrict__ S,
+                                             const double* __restrict__ B, double lambda,
+                                             unsigned long long* __restrict__ resid)
 {
-    __shared__ double sI[F64_KC][F64_TC];
-    __shared__ double sW[F64_KC][F64_TK];
+    constexpr int TK = 16 * NB;
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
     const int64_t c0 = (int64_t)blockIdx.x * F64_TC;
-    const int k0 = k_begin + blockIdx.y * F64_TK;
 
-    double acc[4][8];
+    double acc[NB][8];
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < NB; ++m)
 #pragma unroll
         for (int i = 0; i < 8; ++i) acc[m][i] = 0.0;
 
@@ -87,23 +92,24 @@ scatter_fp64_kernel(const double* __restrict__ illum, const double* __restrict__
             }
             sI[jj][cc] = v;
         }
+        // W chunk: F64_KC x TK, NB per thread
 #pragma unroll
-        for (int q = 0; q < (F64_KC * F64_TK) / F64_THREADS; ++q) {
+        for (int q = 0; q < (F64_KC * TK) / F64_THREADS; ++q) {
             const int p = tid + F64_THREADS * q;
-            const int jj = p / F64_TK, kk = p % F64_TK;
+            const int jj = p / TK, kk = p % TK;
             const int j = j0 + jj, k = k0 + kk;
             sW[jj][kk] = (j < M && k < k_end) ? __ldg(W + (int64_t)j * ldw + k) : 0.0;
         }
         __syncthreads();
 #pragma unroll
         for (int jj = 0; jj < F64_KC; ++jj) {
-            double iv[8], wv[4];
+            double iv[8], wv[NB];
 #pragma unroll
             for (int i = 0; i < 8; ++i) iv[i] = sI[jj][tx + 16 * i];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) wv[m] = sW[jj][ty + 16 * m];
+            for (int m = 0; m < NB; ++m) wv[m] = sW[jj][ty + 16 * m];
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
+            for (int m = 0; m < NB; ++m)
 #pragma unroll
                 for (int i = 0; i < 8; ++i) acc[m][i] = fma(wv[m], iv[i], acc[m][i]);
         }
@@ -112,7 +118,7 @@ scatter_fp64_kernel(const double* __restrict__ illum, const double* __restrict__
 
     double rmax = 0.0;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < NB; ++m) {
         const int k = k0 + ty + 16 * m;
         if (k >= k_end) continue;
 #pragma unroll
@@ -127,6 +133,51 @@ scatter_fp64_kernel(const double* __restrict__ illum, const double* __restrict__
         }
     }
     if (kResidual) residual_max(resid, rmax);
+}
+
+// Grid: x over 128-cell tiles; y over the out-directions [k_begin, k_end),
+// n_full tiles of 64 and then, when the range is not a multiple of 64, one
+// tile of 16*nb_last (nb_last 1..4) for the rest.  The narrow tiles are last
+// in launch order, so they fill the final wave.
+template <bool kUpdate, bool kResidual>
+__global__ void __launch_bounds__(F64_THREADS)
+scatter_fp64_kernel(const double* __restrict__ illum, const double* __restrict__ W, int64_t N,
+                    int M, int ldw, int k_begin, int k_end, int n_full, int nb_last, double* __restrict__ S,
+                    const double* __restrict__ B, double lambda,
+                    unsigned long long* __restrict__ resid)
+{
+    __shared__ double sI[F64_KC][F64_TC];
+    __shared__ double sW[F64_KC][F64_TK];
+    const int k0 = k_begin + (int)blockIdx.y * F64_TK;
+    const int nb = (int)blockIdx.y < n_full ? 4 : nb_last;
+    switch (nb) {
+    case 1:
+        scatter_tile<kUpdate, kResidual, 1>(sI, sW, illum, W, N, M, ldw, k0, k_end, S, B, lambda, resid);
+        break;
+    case 2:
+        scatter_tile<kUpdate, kResidual, 2>(sI, sW, illum, W, N, M, ldw, k0, k_end, S, B, lambda, resid);
+        break;
+    case 3:
+        scatter_tile<kUpdate, kResidual, 3>(sI, sW, illum, W, N, M, ldw, k0, k_end, S, B, lambda, resid);
+        break;
+    default:
+        scatter_tile<kUpdate, kResidual, 4>(sI, sW, illum, W, N, M, ldw, k0, k_end, S, B, lambda, resid);
+        break;
+    }
+}
+
+// The y extent of scatter_fp64_kernel's grid over `width` out-directions.
+struct DirTiles {
+    int n_full, nb_last, gy;
+};
+inline DirTiles dir_tiles(int64_t width)
+{
+    DirTiles t;
+    t.n_full = (int)(width / F64_TK);
+    const int rem = (int)(width % F64_TK);
+    t.nb_last = rem ? (rem + 15) / 16 : 4;
+    t.gy = t.n_full + (rem ? 1 : 0);
+    return t;
 }
 
 __device__ __forceinline__ double gamma_thomson(double ax, double ay, double az, double bx,
@@ -408,23 +459,23 @@ int rts_launch_scatter_fp64(rts_ctx* ctx, int64_t k_begin, int64_t k_end, cudaSt
 {
     if (k_end <= k_begin) return RTS_OK;
     const int64_t gx = (ctx->N + F64_TC - 1) / F64_TC;
-    const int64_t gy = (k_end - k_begin + F64_TK - 1) / F64_TK;
-    RTS_REQUIRE(ctx, gx < (1ll << 31) && gy < 65536, RTS_ERR_UNSUPPORTED, "FP64 grid too large");
-    dim3 grid((unsigned)gx, (unsigned)gy);
+    const DirTiles dt = dir_tiles(k_end - k_begin);
+    RTS_REQUIRE(ctx, gx < (1ll << 31) && dt.gy < 65536, RTS_ERR_UNSUPPORTED, "FP64 grid too large");
+    dim3 grid((unsigned)gx, (unsigned)dt.gy);
     const int ldw = (int)ctx->local();
     rts_timing_begin(ctx, st);
     if (update && residual)
         scatter_fp64_kernel<true, true><<<grid, F64_THREADS, 0, st>>>(
-            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, ctx->d_S, B,
-            lambda, ctx->resid_target);
+            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, dt.n_full, dt.nb_last,
+            ctx->d_S, B, lambda, ctx->resid_target);
     else if (update)
         scatter_fp64_kernel<true, false><<<grid, F64_THREADS, 0, st>>>(
-            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, ctx->d_S, B,
-            lambda, ctx->resid_target);
+            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, dt.n_full, dt.nb_last,
+            ctx->d_S, B, lambda, ctx->resid_target);
     else
         scatter_fp64_kernel<false, false><<<grid, F64_THREADS, 0, st>>>(
-            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, ctx->d_S,
-            nullptr, 0.0, ctx->resid_target);
+            ctx->d_illum, ctx->d_W, ctx->N, (int)ctx->M, ldw, (int)k_begin, (int)k_end, dt.n_full, dt.nb_last,
+            ctx->d_S, nullptr, 0.0, ctx->resid_target);
     rts_timing_end(ctx, st);
     RTS_CHECK_LAUNCH(ctx, "scatter_fp64_kernel");
     ctx->launches++;
@@ -586,9 +637,11 @@ extern "C" int rts_scattering_noalloc(const double* d_illum, const double* d_xyz
     weights_kernel<<<(unsigned)((M + 127) / 128), 128, 0, st>>>(d_xyz, d_area, (int)M, 0, (int)M, full_area,
                                                                 RTS_PHASE_THOMSON, 0.0, W);
     if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;  // nothing was pending: this launch's error
-    dim3 grid((unsigned)gx, (unsigned)((M + F64_TK - 1) / F64_TK));
+    const DirTiles dt = dir_tiles(M);
+    dim3 grid((unsigned)gx, (unsigned)dt.gy);
     scatter_fp64_kernel<false, false><<<grid, F64_THREADS, 0, st>>>(d_illum, W, N, (int)M, (int)M, 0, (int)M,
-                                                                     d_scattering, nullptr, 0.0, nullptr);
+                                                                     dt.n_full, dt.nb_last, d_scattering, nullptr,
+                                                                     0.0, nullptr);
     if (cudaGetLastError() != cudaSuccess) return RTS_ERR_CUDA;
     return RTS_OK;
 }

@@ -39,7 +39,12 @@ def problem(N, M, seed):
     return xyz, area, fa, il, B
 
 
-@pytest.mark.parametrize("N,M", SHAPES)
+# the FP64 kernel's tiles of 64 out-directions and its last, narrower tile:
+# 16 (M = 1, 3, 15, 16, 200), 32 (90), 48 (33), 64 wide (127: 63 used)
+FP64_SHAPES = SHAPES + [(700, 90), (300, 127), (257, 200)]
+
+
+@pytest.mark.parametrize("N,M", FP64_SHAPES)
 def test_fp64_small_shapes(ctx, N, M):
     xyz, area, fa, il, _ = problem(N, M, 3)
     ctx.init(xyz, area, fa, N)
