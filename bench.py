@@ -150,6 +150,7 @@ def run_moments(args, rank, world, local):
     clk = clocks.stop()
     peaks, src = load_peaks()
     hbm = peak_value(peaks, "hbm_gbs") or FALLBACK_PEAKS["hbm_gbs"]
+    fp64_peak = ctx.measure_fp64_peak(2.0)  # this GPU's FP64 FMA rate, after the timed passes
     m = res["illum_params"]
     line = {"metric": "FP64 moment pass Gcell·dir/s", "value": args.cells * 1000 / (m["kernel_ms"] / 1e3) / 1e9,
             "unit": "Gcell·dir/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -157,10 +158,11 @@ def run_moments(args, rank, world, local):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"config 2 Illum ({args.cells} cells x 1000 directions, FP64 faces): moments and "
                                    "fused divergence pass"},
-            "roofline": {"bound": "fp64", "achieved": m["fp64_tflops"], "peak": FP64_NOMINAL_TFLOPS,
-                         "unit": "TFLOP/s", "frac": m["fp64_tflops"] / FP64_NOMINAL_TFLOPS, "traffic": None,
+            "roofline": {"bound": "fp64", "achieved": m["fp64_tflops"], "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": m["fp64_tflops"] / fp64_peak, "traffic": None,
                          "hbm_gbs": m["hbm_gbs"], "hbm_frac": m["hbm_gbs"] / hbm,
-                         "peak_source": f"nominal GB300 FP64; HBM {src}"},
+                         "peak_source": f"measured FP64 FMA rate of this GPU (rts_measure_fp64_peak); HBM {src}",
+                         "nominal_fp64_tflops": FP64_NOMINAL_TFLOPS},
             "result": res, "clocks": clk}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -296,10 +298,12 @@ def run_sweep(args, rank, world, local):
     prof = read_sweep_profile()
     fl = prof.get("fp64_flops_per_cell_dir")
     achieved = fl * value * 1e9 / 1e12 if fl else None
-    roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-            "frac": achieved / FP64_NOMINAL_TFLOPS if achieved else None,
+    fp64_peak = ctx.measure_fp64_peak(2.0)  # this GPU's FP64 FMA rate, after the timed sweeps
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak if achieved else None,
             "traffic": prof.get("dram_bytes_per_cell_dir") and prof["dram_bytes_per_cell_dir"] * N * M,
-            "peak_source": "nominal GB300 FP64 (no measured FP64 peak available)",
+            "peak_source": "measured FP64 FMA rate of this GPU (rts_measure_fp64_peak)",
+            "nominal_fp64_tflops": FP64_NOMINAL_TFLOPS,
             "fp64_pipe_active": prof.get("fp64_pipe_active_frac"),
             "note": "achieved = FP64 operations per cell-direction of the read form counted by ncu "
                     "(dadd + dmul + 2 dfma) x the measured cell-direction rate; the pipe also issues the compares, "
@@ -766,9 +770,10 @@ def run_ours(args, rank, world, local):
     achieved = flops / kern_avg / 1e12 if kern_n else None
     traffic = read_traffic().get(f"{prec}:{N}x{M}")
     if prec == "fp64":
-        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                "frac": achieved / FP64_NOMINAL_TFLOPS if achieved else None, "traffic": traffic,
-                "peak_source": "nominal GB300 FP64 (no measured FP64 peak available)"}
+        roof = {"bound": "fp64", "achieved": achieved, "peak": measured["fp64_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / measured["fp64_tflops"] if achieved else None, "traffic": traffic,
+                "peak_source": "measured FP64 FMA rate of this GPU (rts_measure_fp64_peak)",
+                "nominal_fp64_tflops": FP64_NOMINAL_TFLOPS}
     else:
         pk = peak_value(peaks, "bf16_tflops") or FALLBACK_PEAKS["bf16_tflops"]
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s",
