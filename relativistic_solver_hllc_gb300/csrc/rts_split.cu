@@ -240,6 +240,16 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
 // the host-buffer call's ranges would only multiply the launches.  The
 // range's problem is the host-buffer call's first (rebuilt when the call
 // alternates with host-buffer calls).
+static int ensure_staging(rts_ctx* ctx);
+static int record_on(rts_ctx* ctx, cudaEvent_t& ev, cudaStream_t st);
+
+// The scattering integral of the device Illum into the FP64 device S (all
+// out-directions), on `st`, for the on-device source iteration.  The rows
+// come from the staged preparation (one read of the Illum into FP64 face
+// sums and per-cell maxima, then scales and split on the integer pipe), bit
+// for bit the rows of the direct one.  Its staging is the asynchronous
+// calls': it waits for their preparation and face sums in flight, and leaves
+// them to prepare their rows again.
 int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
 {
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
@@ -249,7 +259,12 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     const int flush = rts_ctx_flush(ctx, precision);
     const int nch = 1;
     const int64_t csz = N;
-    int rc;
+    int rc = ensure_staging(ctx);
+    if (rc != RTS_OK) return rc;
+    if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
+    if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
+    s.call_version = -1;
+    s.eager_next = -1;
     for (int i = 0; i < nch; ++i) {
         const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
         if (n <= 0) break;
@@ -262,28 +277,33 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
         p->use_B = false;
         if (changed) rts_group_invalidate(s.chunk[i]);
         if ((rc = rts_group_prepare(s.chunk[i], 0, st)) != RTS_OK) return rc;
-        rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode, p->rs,
-                                    p->rows_pad, p->a[0], st);
+        rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode,
+                                           p->rs, p->rows_pad, p->a[0], s.call_sums, s.call_max, st);
+        // later preparations and face sums of the asynchronous calls wait for this one's
+        if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
         if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, st);
         if (rc != RTS_OK) return rc;
     }
     return RTS_OK;
 }
 
-// rts_scattering_async at a tensor precision: local out-directions
-// [start, end) of the device Illum into rows [start, end) of the FP64 device
-// S, on `st`.  Stream slot `slot` keeps its own one-problem batch (split
-// Ibar rows, row scales, the split W columns [start, end), table, residual),
-// rebuilt when the range, shape, precision or flush period changes and its W
-// split again when the context's W changed.  Two calls queued on different
-// slots at once -- the reference's pair [0, size_1) on scattering stream 1
-// and [0, local) on scattering stream 2 -- therefore write no common buffer
-// except the rows of S they share, into which both write the same values
-// (each output's arithmetic does not depend on the tiling of the
-// out-directions).  After the first call of a slot nothing synchronises the
-// host.
-// Frees the split Ibar rows shared by the asynchronous calls' slots (cudaFree
-// waits for the device, so no contraction still reads them).
+// rts_scattering_async at a tensor precision (rts_split_async below): local
+// out-directions [start, end) of the device Illum into rows [start, end) of
+// the FP64 device S, on `st`.  Stream slot `slot` keeps its own one-problem
+// batch (the split W columns [start, end), table, residual), rebuilt when the
+// range, shape, precision or flush period changes and its W split again when
+// the context's W changed.  The split Ibar rows and their row scales depend
+// on the Illum only and are shared by the slots: a call prepares them, and
+// the next call on each other slot waits on that preparation's event and
+// reads them.  Two calls queued on different slots at once -- the
+// reference's pair [0, size_1) on scattering stream 1 and [0, local) on
+// scattering stream 2 -- therefore write no common buffer except the rows of
+// S they share, into which both write the same values (each output's
+// arithmetic does not depend on the tiling of the out-directions).  After the
+// first call of a slot nothing synchronises the host.
+//
+// Frees the shared split Ibar rows and the staging (cudaFree waits for the
+// device, so no contraction still reads them).
 static void free_call_rows(rts_ctx* ctx)
 {
     rts_split_state& s = ctx->split;
@@ -307,6 +327,25 @@ static void free_call_rows(rts_ctx* ctx)
 // The shared rows for (N, M, mode): allocated on first use and when the
 // precision or the sizes change (the slots' problems, whose tensor maps hold
 // the old address, are rebuilt: slot_gen).
+// The staging of the staged preparation alone: FP64 face sums [M][N] and
+// per-cell maxima [N] (kept with the shared rows when those exist).
+static int ensure_staging(rts_ctx* ctx)
+{
+    rts_split_state& s = ctx->split;
+    const size_t ibytes = (size_t)(ctx->M * ctx->N * 8), mbytes = (size_t)(ctx->N * 8);
+    if (s.call_sums && s.call_sums_bytes == ibytes && s.call_max_bytes == mbytes) return RTS_OK;
+    free_call_rows(ctx);
+    void *ib = nullptr, *mx = nullptr;
+    int rc = rts_dmalloc(ctx, &ib, ibytes, "FP64 face sums (staging)");
+    if (rc == RTS_OK) rc = rts_dmalloc(ctx, &mx, mbytes, "per-cell maxima (staging)");
+    s.call_sums = (double*)ib;
+    s.call_max = (unsigned long long*)mx;
+    s.call_sums_bytes = ib ? ibytes : 0;
+    s.call_max_bytes = mx ? mbytes : 0;
+    if (rc != RTS_OK) free_call_rows(ctx);
+    return rc;
+}
+
 static int ensure_call_rows(rts_ctx* ctx, int mode, int64_t rows_pad, int64_t units)
 {
     rts_split_state& s = ctx->split;
@@ -451,6 +490,8 @@ int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int
         for (int i = 0; i < RTS_STREAM_COUNT; ++i)
             if (i != slot && s.use_recorded[i]) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_use[i], 0));
         if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
+        // and the staging by the device source iteration's preparation
+        if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
         s.call_version = -1;
         // the face sums of this Illum, when its copies summed every direction
         const bool eager = s.eager_next == M && s.eager_mode == mode && s.eager_version == ctx->inputs_version;

@@ -163,6 +163,49 @@ def test_illum_solve_hg_phase(ctx, precision, tol):
     assert rel_err(got, il.ravel()) <= tol, rel_err(got, il.ravel())
 
 
+def test_illum_solve_and_the_calls_share_the_staging(ctx):
+    """The device source iteration at a tensor precision prepares its rows
+    in the staging of the asynchronous integral calls (FP64 face sums and
+    per-cell maxima).  With the iteration between them, the calls still give
+    the values they give alone: the pair of calls on the Illum the iteration
+    left equals the host-buffer call on that Illum bit for bit (another
+    preparation, the same rows), and the pair on the first Illum again
+    repeats its first result."""
+    M = 30
+    S1, S2 = _native.STREAM_SCATTERING_1, _native.STREAM_SCATTERING_2
+    vert, pairs, normals, xyz, area, fa, N = setup(ctx, 4, M)
+    ctx.sweep_build()
+    a, b, q = coefficients(N, 2, "class1")
+    ctx.sweep_set_medium(medium(), a, b, q, (0.0, 0.0, 1.0, 0.0))
+    il0 = np.random.default_rng(5).uniform(0.1, 1.0, M * N * 4)
+
+    def pair():
+        out1, out2 = np.zeros(M * N), np.zeros(M * N)
+        ctx.scattering_async(0, M // 3, S1, out1)
+        ctx.scattering_async(0, M, S2, out2)
+        ctx.wait()
+        assert np.array_equal(out1[: (M // 3) * N], out2[: (M // 3) * N])
+        return out2
+
+    ctx.set_precision("fp16x3")
+    try:
+        ctx.copy_illum(il0)
+        first = pair()
+        ctx.illum_solve("fp16x3", max_iter=3, accuracy=1e-300)
+        il1 = np.empty(M * N * 4)
+        ctx.read_illum(il1)
+        after = pair()
+        host_call = ctx.scattering(il1)
+        ctx.copy_illum(il0)
+        again = pair()
+    finally:
+        ctx.set_precision("fp64")
+    assert np.array_equal(after, host_call.ravel())
+    assert np.array_equal(again, first)
+    assert rel_err(after.reshape(M, N), oracle.calculate_int_cpu(N, xyz, area, fa, il1)) <= 1e-6
+    assert rel_err(first.reshape(M, N), oracle.calculate_int_cpu(N, xyz, area, fa, il0)) <= 1e-6
+
+
 def test_stored_attenuation_factors_give_the_same_sweep(ctx):
     """The sweep that stores the nodes' attenuation factors, the sweeps that
     read them and the sweeps that evaluate them (RTS_TUNE_SWEEP_CACHE 0) give
