@@ -27,7 +27,7 @@ def build_driver(out_dir):
 
 
 def test_compat_shim_compiles_against_standin(native_lib, tmp_path):
-    """CPU check: the shim and the driver compile and link against the library."""
+    """CPU check: the shim and its calling-sequence program compile and link against the library."""
     assert build_driver(tmp_path).exists()
 
 
