@@ -241,6 +241,7 @@ int rts_split_host_call(rts_ctx* ctx, int precision, const double* illum_host, c
 // range's problem is the host-buffer call's first (rebuilt when the call
 // alternates with host-buffer calls).
 static int ensure_staging(rts_ctx* ctx);
+static bool no_room(int rc);
 static int record_on(rts_ctx* ctx, cudaEvent_t& ev, cudaStream_t st);
 
 // The scattering integral of the device Illum into the FP64 device S (all
@@ -249,7 +250,8 @@ static int record_on(rts_ctx* ctx, cudaEvent_t& ev, cudaStream_t st);
 // sums and per-cell maxima, then scales and split on the integer pipe), bit
 // for bit the rows of the direct one.  Its staging is the asynchronous
 // calls': it waits for their preparation and face sums in flight, and leaves
-// them to prepare their rows again.
+// them to prepare their rows again.  Without room for the staging (HBM
+// budget or memory) the rows are prepared directly.
 int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
 {
     RTS_REQUIRE(ctx, ctx->cc_major == 10, RTS_ERR_UNSUPPORTED, "the tensor-core path needs a Blackwell (sm_10x) device");
@@ -260,11 +262,14 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     const int nch = 1;
     const int64_t csz = N;
     int rc = ensure_staging(ctx);
-    if (rc != RTS_OK) return rc;
-    if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
-    if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
-    s.call_version = -1;
-    s.eager_next = -1;
+    const bool staged = rc == RTS_OK;
+    if (!staged && !no_room(rc)) return rc;
+    if (staged) {
+        if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
+        if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
+        s.call_version = -1;
+        s.eager_next = -1;
+    }
     for (int i = 0; i < nch; ++i) {
         const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
         if (n <= 0) break;
@@ -277,10 +282,15 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
         p->use_B = false;
         if (changed) rts_group_invalidate(s.chunk[i]);
         if ((rc = rts_group_prepare(s.chunk[i], 0, st)) != RTS_OK) return rc;
-        rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode,
-                                           p->rs, p->rows_pad, p->a[0], s.call_sums, s.call_max, st);
-        // later preparations and face sums of the asynchronous calls wait for this one's
-        if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
+        if (staged) {
+            rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode,
+                                               p->rs, p->rows_pad, p->a[0], s.call_sums, s.call_max, st);
+            // later preparations and face sums of the asynchronous calls wait for this one's
+            if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
+        } else {
+            rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode, p->rs,
+                                        p->rows_pad, p->a[0], st);
+        }
         if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, st);
         if (rc != RTS_OK) return rc;
     }
@@ -327,24 +337,36 @@ static void free_call_rows(rts_ctx* ctx)
 // The shared rows for (N, M, mode): allocated on first use and when the
 // precision or the sizes change (the slots' problems, whose tensor maps hold
 // the old address, are rebuilt: slot_gen).
-// The staging of the staged preparation alone: FP64 face sums [M][N] and
-// per-cell maxima [N] (kept with the shared rows when those exist).
+// The staging of the staged preparation: FP64 face sums [M][N] and per-cell
+// maxima [N].  When it does not fit (RTS_ERR_OVER_BUDGET or
+// RTS_ERR_OUT_OF_MEMORY) it stays absent and the callers prepare the rows
+// directly from the faces, which gives the same rows bit for bit.
 static int ensure_staging(rts_ctx* ctx)
 {
     rts_split_state& s = ctx->split;
     const size_t ibytes = (size_t)(ctx->M * ctx->N * 8), mbytes = (size_t)(ctx->N * 8);
     if (s.call_sums && s.call_sums_bytes == ibytes && s.call_max_bytes == mbytes) return RTS_OK;
-    free_call_rows(ctx);
+    rts_dfree(ctx, s.call_sums, s.call_sums_bytes);  // cudaFree waits for the device
+    rts_dfree(ctx, s.call_max, s.call_max_bytes);
+    s.call_sums = nullptr;
+    s.call_max = nullptr;
+    s.call_sums_bytes = s.call_max_bytes = 0;
+    s.eager_next = -1;
     void *ib = nullptr, *mx = nullptr;
     int rc = rts_dmalloc(ctx, &ib, ibytes, "FP64 face sums (staging)");
     if (rc == RTS_OK) rc = rts_dmalloc(ctx, &mx, mbytes, "per-cell maxima (staging)");
+    if (rc != RTS_OK) {
+        rts_dfree(ctx, ib, ib ? ibytes : 0);
+        return rc;
+    }
     s.call_sums = (double*)ib;
     s.call_max = (unsigned long long*)mx;
-    s.call_sums_bytes = ib ? ibytes : 0;
-    s.call_max_bytes = mx ? mbytes : 0;
-    if (rc != RTS_OK) free_call_rows(ctx);
-    return rc;
+    s.call_sums_bytes = ibytes;
+    s.call_max_bytes = mbytes;
+    return RTS_OK;
 }
+
+static bool no_room(int rc) { return rc == RTS_ERR_OVER_BUDGET || rc == RTS_ERR_OUT_OF_MEMORY; }
 
 static int ensure_call_rows(rts_ctx* ctx, int mode, int64_t rows_pad, int64_t units)
 {
@@ -352,22 +374,17 @@ static int ensure_call_rows(rts_ctx* ctx, int mode, int64_t rows_pad, int64_t un
     if (s.call_a && s.call_mode == mode && s.call_N == ctx->N && s.call_M == ctx->M) return RTS_OK;
     free_call_rows(ctx);
     const size_t abytes = (size_t)(rows_pad * units * 2), rbytes = (size_t)(2 * rows_pad * 4);
-    const size_t ibytes = (size_t)(ctx->M * ctx->N * 8), mbytes = (size_t)(ctx->N * 8);
-    void *a = nullptr, *r = nullptr, *ib = nullptr, *mx = nullptr;
+    void *a = nullptr, *r = nullptr;
     int rc = rts_dmalloc(ctx, &a, abytes, "split Ibar rows of the integral calls");
     if (rc == RTS_OK) rc = rts_dmalloc(ctx, &r, rbytes, "row scales of the integral calls");
-    if (rc == RTS_OK) rc = rts_dmalloc(ctx, &ib, ibytes, "FP64 face sums (staging)");
-    if (rc == RTS_OK) rc = rts_dmalloc(ctx, &mx, mbytes, "per-cell maxima (staging)");
     s.call_a = (uint16_t*)a;
     s.call_rs = (float*)r;
-    s.call_sums = (double*)ib;
-    s.call_max = (unsigned long long*)mx;
     s.call_a_bytes = a ? abytes : 0;
     s.call_rs_bytes = r ? rbytes : 0;
-    s.call_sums_bytes = ib ? ibytes : 0;
-    s.call_max_bytes = mx ? mbytes : 0;
     if (rc == RTS_OK && cudaMemset(a, 0, abytes) != cudaSuccess)  // padding rows stay zero
         rc = rts_fail(ctx, RTS_ERR_CUDA, "clearing the shared split rows failed");
+    // the staging is optional: without room for it the calls prepare directly
+    if (rc == RTS_OK && (rc = ensure_staging(ctx)) != RTS_OK && no_room(rc)) rc = RTS_OK;
     if (rc != RTS_OK) {
         free_call_rows(ctx);
         return rc;
@@ -406,6 +423,10 @@ int rts_split_eager_send(rts_ctx* ctx, int64_t shift_dev, int64_t size)
     rts_group_geometry(M, M, ctx->N, 0, &bn, &n_tiles, &kpad, &mpad, &rows_pad, &m_tiles);
     int rc = ensure_call_rows(ctx, mode, rows_pad, (mode == 2 ? 4 : 2) * kpad);
     if (rc != RTS_OK) return rc;
+    if (!s.call_sums) {  // no staging: this Illum is prepared directly at the call
+        s.eager_next = -1;
+        return RTS_OK;
+    }
     if (!s.eager_st) RTS_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s.eager_st, cudaStreamNonBlocking));
     cudaStream_t s1 = ctx->streams[RTS_STREAM_SCATTERING_1];
     if (j0 == 0) {
@@ -494,13 +515,17 @@ int rts_split_async(rts_ctx* ctx, int precision, int64_t start, int64_t end, int
         if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
         s.call_version = -1;
         // the face sums of this Illum, when its copies summed every direction
-        const bool eager = s.eager_next == M && s.eager_mode == mode && s.eager_version == ctx->inputs_version;
+        const bool eager = s.call_sums && s.eager_next == M && s.eager_mode == mode &&
+                           s.eager_version == ctx->inputs_version;
         if (eager)
             rc = rts_pp_rows_from_sums(ctx, N, (int)M, (int)kpad, nullptr, mode, s.call_rs, rows_pad, s.call_a,
                                        s.call_sums, s.call_max, st);
-        else
+        else if (s.call_sums)
             rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum, N, N, (int)M, (int)kpad, nullptr, mode, s.call_rs,
                                                rows_pad, s.call_a, s.call_sums, s.call_max, st);
+        else
+            rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)M, (int)kpad, nullptr, mode, s.call_rs, rows_pad,
+                                        s.call_a, st);
         if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
         if (rc != RTS_OK) return rc;
         s.call_version = ctx->inputs_version;

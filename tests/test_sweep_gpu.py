@@ -206,6 +206,53 @@ def test_illum_solve_and_the_calls_share_the_staging(ctx):
     assert rel_err(first.reshape(M, N), oracle.calculate_int_cpu(N, xyz, area, fa, il0)) <= 1e-6
 
 
+def test_no_room_for_the_staging(ctx):
+    """Under an HBM budget with room for everything the tensor-precision
+    source iteration and the integral calls hold except the staging of the
+    staged preparation, both prepare their rows directly from the faces: the
+    same norms, Illum and integrals bit for bit."""
+    M = 30
+    S1, S2 = _native.STREAM_SCATTERING_1, _native.STREAM_SCATTERING_2
+    il0 = None
+
+    def run(room=None):
+        nonlocal il0
+        vert, pairs, normals, xyz, area, fa, N = setup(ctx, 4, M)
+        ctx.sweep_build()
+        a, b, q = coefficients(N, 2, "class1")
+        ctx.sweep_set_medium(medium(), a, b, q, (0.0, 0.0, 1.0, 0.0))
+        if il0 is None:
+            il0 = np.random.default_rng(6).uniform(0.1, 1.0, M * N * 4)
+        ctx.copy_illum(np.zeros(M * N * 4))  # the first norm compares against it
+        used0 = ctx.hbm_used()
+        if room is not None:
+            ctx.set_hbm_budget(used0 + room)
+        norms = ctx.illum_solve("fp16x3", max_iter=3, accuracy=1e-300)
+        il = np.empty(M * N * 4)
+        ctx.read_illum(il)
+        ctx.set_precision("fp16x3")
+        try:
+            ctx.copy_illum(il0)
+            out1, out2 = np.zeros(M * N), np.zeros(M * N)
+            ctx.scattering_async(0, M // 3, S1, out1)
+            ctx.scattering_async(0, M, S2, out2)
+            ctx.wait()
+        finally:
+            ctx.set_precision("fp64")
+        return N, ctx.hbm_used() - used0, list(norms), il, out2
+
+    try:
+        N, held, n1, il1, out1 = run()
+        staging = M * N * 8 + N * 8
+        _, held2, n2, il2, out2 = run(held - staging // 2)
+    finally:
+        ctx.set_hbm_budget(1 << 62)
+    assert held2 <= held - staging  # the staging was not allocated
+    assert n1 == n2
+    assert np.array_equal(il1, il2)
+    assert np.array_equal(out1, out2)
+
+
 def test_stored_attenuation_factors_give_the_same_sweep(ctx):
     """The sweep that stores the nodes' attenuation factors, the sweeps that
     read them and the sweeps that evaluate them (RTS_TUNE_SWEEP_CACHE 0) give
