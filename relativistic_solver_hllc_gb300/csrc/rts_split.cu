@@ -57,6 +57,7 @@ int build_problem(rts_ctx* ctx, rts_batch** pb, int64_t* id, int precision, bool
     p->cur = 0;
     p->S64 = S64;
     p->use_B = B_dev != nullptr;
+    // once per set-up: the direct preparation, which needs no staging
     int rc = rts_pp_rows_from_faces(ctx, ctx->d_illum, N, N, (int)Min, (int)p->kpad, B_dev, mode, p->rs, p->rows_pad,
                                     p->a[0], st, p->part != nullptr);
     if (rc != RTS_OK) return rc;
@@ -244,6 +245,31 @@ static int ensure_staging(rts_ctx* ctx);
 static bool no_room(int rc);
 static int record_on(rts_ctx* ctx, cudaEvent_t& ev, cudaStream_t st);
 
+// Rows of cells [0, n) of a device Illum whose rows hold `ld` cells into A and
+// rs on `st`: the staged preparation in the integral calls' staging (waiting
+// for their preparation and face sums in flight, and leaving them to prepare
+// their own rows again), or, without room for the staging, the direct one.
+// The two give the same rows bit for bit.
+static int prepare_device_rows(rts_ctx* ctx, const double* illum, int64_t n, int64_t ld, int M, int kpad,
+                               const double* B, int mode, float* rs, int64_t npad, uint16_t* A, cudaStream_t st,
+                               bool bound)
+{
+    rts_split_state& s = ctx->split;
+    int rc = ensure_staging(ctx);
+    if (rc != RTS_OK) {
+        if (!no_room(rc)) return rc;
+        return rts_pp_rows_from_faces(ctx, illum, n, ld, M, kpad, B, mode, rs, npad, A, st, bound);
+    }
+    if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
+    if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
+    s.call_version = -1;
+    s.eager_next = -1;
+    rc = rts_pp_rows_from_faces_staged(ctx, illum, n, ld, M, kpad, B, mode, rs, npad, A, s.call_sums, s.call_max, st,
+                                       bound);
+    if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);  // later users of the staging wait for this one
+    return rc;
+}
+
 // The scattering integral of the device Illum into the FP64 device S (all
 // out-directions), on `st`, for the on-device source iteration.  The rows
 // come from the staged preparation (one read of the Illum into FP64 face
@@ -261,15 +287,7 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
     const int flush = rts_ctx_flush(ctx, precision);
     const int nch = 1;
     const int64_t csz = N;
-    int rc = ensure_staging(ctx);
-    const bool staged = rc == RTS_OK;
-    if (!staged && !no_room(rc)) return rc;
-    if (staged) {
-        if (s.ev_prep) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_prep, 0));
-        if (s.ev_eager) RTS_CUDA_TRY(ctx, cudaStreamWaitEvent(st, s.ev_eager, 0));
-        s.call_version = -1;
-        s.eager_next = -1;
-    }
+    int rc;
     for (int i = 0; i < nch; ++i) {
         const int64_t c0 = i * csz, n = std::min(N, c0 + csz) - c0;
         if (n <= 0) break;
@@ -282,15 +300,8 @@ int rts_split_device_call(rts_ctx* ctx, int precision, cudaStream_t st)
         p->use_B = false;
         if (changed) rts_group_invalidate(s.chunk[i]);
         if ((rc = rts_group_prepare(s.chunk[i], 0, st)) != RTS_OK) return rc;
-        if (staged) {
-            rc = rts_pp_rows_from_faces_staged(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode,
-                                               p->rs, p->rows_pad, p->a[0], s.call_sums, s.call_max, st);
-            // later preparations and face sums of the asynchronous calls wait for this one's
-            if (rc == RTS_OK) rc = record_on(ctx, s.ev_prep, st);
-        } else {
-            rc = rts_pp_rows_from_faces(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode, p->rs,
-                                        p->rows_pad, p->a[0], st);
-        }
+        rc = prepare_device_rows(ctx, ctx->d_illum + c0 * 4, n, N, (int)M, (int)p->kpad, nullptr, mode, p->rs,
+                                 p->rows_pad, p->a[0], st, false);
         if (rc == RTS_OK) rc = rts_group_step(s.chunk[i], 0, st);
         if (rc != RTS_OK) return rc;
     }
