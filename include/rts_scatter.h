@@ -142,7 +142,11 @@ int rts_copy_illum(rts_ctx* ctx, int64_t size, const double* illum_host);
  * RTS_PREC_TF32X3 to 1e-6 relative, RTS_PREC_BF16X3 to ~1e-5): the
  * reference's kernel d_GetS_MPI_Stream at that precision, behind the same
  * call.  RTS_ERR_UNSUPPORTED for a tensor precision on a device other than
- * sm_10x. */
+ * sm_10x.  At a tensor precision the calls also hold the split Ibar rows
+ * (4 bytes per cell and in-direction, 8 for RTS_PREC_TF32X3) and, where the
+ * HBM budget and the device leave room, a staging of the FP64 face sums
+ * (8 bytes per cell and direction) that speeds up their preparation; without
+ * that room the rows are prepared directly, with the same results. */
 int rts_set_precision(rts_ctx* ctx, int precision);
 int rts_get_precision(const rts_ctx* ctx, int* precision);
 
